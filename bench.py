@@ -1,0 +1,404 @@
+"""Voronoi cells/sec on one GB300: FP32+FP64-guard (default) or plain FP64,
+next to the host-CPU oracle.
+
+A step is one pass of the hot path over the workload: bin the points
+(bounds, histogram, scan, scatter, shell table), clip every cell, re-run the
+flagged cells, and compact the per-cell face lists into CSR.  `value` has the
+points already in HBM; `e2e` goes through the C ABI with pinned host buffers:
+upload the points, compute, read back volumes and the neighbour/area CSR.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload uniform16m|uniform1m|clustered|sc|bcc|batched] [--precision fp32|fp64]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "the-tessellator_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "cells/sec on 1 GB300: FP32+FP64-guard vs plain FP64 at vol err <=1e-6, vs host CPU"
+WORKLOADS = {
+    "uniform16m": dict(n=16_777_216, seed=2, desc="16,777,216 points i.i.d. uniform in [0,1]^3 (seed 2)"),
+    "uniform1m": dict(n=1_000_000, seed=1, desc="1,000,000 points i.i.d. uniform in [0,1]^3 (seed 1)"),
+    "clustered": dict(n=4_194_304, seed=3, desc="4,194,304 points: 64 Gaussians sigma 0.01 + 10% uniform (seed 3)"),
+    "sc": dict(n=128 ** 3, seed=5, desc="simple cubic 128^3, jitter 1e-7 spacing (seed 5)"),
+    "bcc": dict(n=2 * 100 ** 3, seed=6, desc="BCC 2x100^3, jitter 1e-7 spacing (seed 6)"),
+    "batched": dict(n=None, seed=4, desc="4,096 diagrams, n log-uniform in [64, 65536], boxes [0.5,2]^3 (seed 4)"),
+}
+
+
+def make_points(name):
+    from tessellator import workloads as W
+
+    w = WORKLOADS[name]
+    if name.startswith("uniform"):
+        return W.uniform(w["n"], w["seed"]), None
+    if name == "clustered":
+        return W.clustered(w["n"], w["seed"]), None
+    if name == "sc":
+        return W.lattice_sc(128, w["seed"]), None
+    if name == "bcc":
+        return W.lattice_bcc(100, w["seed"]), None
+    pts, offs, boxes = W.batched(4096, w["seed"])
+    return pts, (offs, boxes)
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas: every rank computes its own copy of the
+# workload on its own GPU; no data exchange)
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws, backend):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, value: float, device=None) -> float:
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = float(f[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.remove(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle on a bounded sample of the same workload
+# ---------------------------------------------------------------------------
+def cpu_baseline(pts, batched, target_seconds=15.0, threads=0):
+    import oracle
+
+    n = len(pts)
+    if batched is not None:
+        offs, boxes = batched
+        # sample whole diagrams until the budget is used
+        t0 = time.perf_counter()
+        cells = 0
+        stats = oracle.CellStats()
+        for d in range(len(offs) - 1):
+            a, b = int(offs[d]), int(offs[d + 1])
+            r = oracle.Diagram(pts[a:b], lo=boxes[d, :3], hi=boxes[d, 3:])
+            _, _, _, _, st, _ = r.compute_all(nthreads=threads)
+            cells += b - a
+            for f in ("candidates", "classified", "cuts", "new_vertices", "fan_triangles", "faces"):
+                setattr(stats, f, getattr(stats, f) + getattr(st, f))
+            if time.perf_counter() - t0 > target_seconds:
+                break
+        secs = time.perf_counter() - t0
+        return cells / secs, stats, cells, f"{cells} cells of the first diagrams, grid build included"
+    t0 = time.perf_counter()
+    r = oracle.Diagram(pts, lo=[0, 0, 0], hi=[1, 1, 1])
+    t_build = time.perf_counter() - t0
+    # calibrate the sample size on a small subset, then run ~target_seconds
+    probe = np.arange(0, n, max(1, n // 20000), dtype=np.uint32)
+    _, _, _, _, st, secs = r.compute_all(nthreads=threads, subset=probe)
+    rate = len(probe) / max(secs, 1e-9)
+    m = int(min(n, max(len(probe), rate * max(1.0, target_seconds - t_build))))
+    sample = np.linspace(0, n - 1, m).astype(np.uint32)
+    _, _, _, _, st, secs = r.compute_all(nthreads=threads, subset=sample)
+    per_cell = secs / m
+    whole = t_build + per_cell * n
+    return n / whole, st, m, (f"{m} of {n} cells (evenly spaced) after the full grid build "
+                              f"({t_build:.2f} s); cells/s = n / (build + n x per-cell time)")
+
+
+def flops_per_cell(st, cells):
+    """Algorithmic FP32 work per cell from the oracle's counters: bisector 12,
+    classify 6 per vertex, intersection 13, fan triangle 12, volume dot 3 per
+    face."""
+    return (12 * st.candidates + 6 * st.classified + 13 * st.new_vertices + 12 * st.fan_triangles
+            + 3 * st.faces) / max(cells, 1)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, ws, rank, local):
+    import torch
+
+    import tessellator as T
+
+    torch.cuda.set_device(local)
+    dist = dist_init(ws, "nccl")
+    pts, batched = make_points(args.workload)
+    n = len(pts)
+    stream = torch.cuda.Stream()
+    cfg = T.default_config(flags=T.FLAG_TIMING, stream=stream.cuda_stream, device=local)
+    prec = args.precision
+    host = torch.from_numpy(pts).pin_memory()
+    dev = host.to(f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    if batched is not None:
+        offs, boxes = batched
+        obj = T.Batch(pts, offs, boxes, config=cfg)
+
+        def step_device():
+            obj.compute(prec)
+
+        def stats():
+            return obj.stats()
+    else:
+        obj = T.Diagram(device_ptr=dev.data_ptr(), n=n, container=T.Polyhedron(0, 0, 0, 1, 1, 1), config=cfg)
+
+        def step_device():
+            obj.rebuild()
+            obj.compute_all(prec)
+            obj.results_device()
+
+        def stats():
+            return obj.stats()
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    st0 = stats()
+    sampler = ClockSampler(local)
+    sampler.start()
+    clip_ms, grid_ms, rerun_ms, csr_ms = [], [], [], []
+    barrier(dist)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_device()
+        s = stats()
+        clip_ms.append(s["ms_clip"])
+        grid_ms.append(s["ms_grid"])
+        rerun_ms.append(s["ms_rerun"])
+        csr_ms.append(s["ms_csr"])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    st1 = stats()
+    ms = max_over_ranks(dist, ms, f"cuda:{local}")
+    launches = int(st1["launches"] - st0["launches"])
+
+    # e2e through the C ABI with pinned host buffers
+    e2e = None
+    if batched is None:
+        L = T.lib()
+        vol_h = torch.empty(n, dtype=torch.float64).pin_memory()
+        offs_h = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+        cap = int(st1["faces"] * 1.2) + 1024
+        nbr_h = torch.empty(cap, dtype=torch.int32).pin_memory()
+        area_h = torch.empty(cap, dtype=torch.float64).pin_memory()
+
+        def step_e2e():
+            T._capi.check(L.tess_diagram_update_points(obj._h, C.c_void_p(host.data_ptr()), 0))
+            T._capi.check(L.tess_diagram_compute_all(obj._h, T._PREC[prec], -1.0, -1))
+            T._capi.check(L.tess_volumes(obj._h, C.cast(vol_h.data_ptr(), C.POINTER(C.c_double))))
+            tot = C.c_size_t(0)
+            T._capi.check(L.tess_neighbors_csr(obj._h, C.cast(offs_h.data_ptr(), C.POINTER(C.c_uint64)),
+                                               C.cast(nbr_h.data_ptr(), C.POINTER(C.c_int32)),
+                                               C.cast(area_h.data_ptr(), C.POINTER(C.c_double)), cap,
+                                               C.byref(tot)))
+            return tot.value
+
+        for _ in range(max(1, args.warmup // 2)):
+            step_e2e()
+        torch.cuda.synchronize()
+        barrier(dist)
+        t0 = time.perf_counter()
+        tot = 0
+        for _ in range(args.steps):
+            tot = step_e2e()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        e2e_s = max_over_ranks(dist, e2e_s, f"cuda:{local}")
+        e2e = {"value": n * ws / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": int(pts.nbytes),
+               "d2h_bytes_per_step": int(8 * n + 8 * (n + 1) + 12 * tot), "ms_per_step": e2e_s * 1e3}
+
+    value = n * ws / (ms / 1e3)
+    out = {
+        "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if prec == "fp32" else "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload]["desc"], "cells": n, "precision":
+                   "FP32 + FP64 guard re-run" if prec == "fp32" else "FP64", "parallelism": "replicas",
+                   "l2": "inputs (%.0f MB of points) larger than the 129 MB L2" % (pts.nbytes / 1e6),
+                   "step": "bin + clip + re-runs + CSR compaction, inputs resident in HBM"},
+        "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
+        "passes_ms": {"grid": float(np.mean(grid_ms)), "clip_first_pass": float(np.mean(clip_ms)),
+                      "reruns": float(np.mean(rerun_ms)), "csr": float(np.mean(csr_ms))},
+        "reruns": {"fp64": int(st1["rerun_fp64"]), "capacity": int(st1["rerun_capacity"]),
+                   "failed": int(st1["failed"])},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, ost, sample_cells, sample_desc = cpu_baseline(pts, batched, args.cpu_seconds)
+        out["cpu_baseline"] = {"value": rate, "unit": "cells/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": sample_desc}
+        fpc = flops_per_cell(ost, sample_cells)
+        peaks, src = measured_peaks()
+        nsm = torch.cuda.get_device_properties(local).multi_processor_count
+        sm_mhz = clocks["sm_mhz"] or peaks.get("sm_max_mhz", 2070.0)
+        peak_fp32 = nsm * 128 * 2 * sm_mhz * 1e6 / 1e12
+        if batched is None:
+            achieved = fpc * n / (np.mean(clip_ms) / 1e3) / 1e12
+            out["roofline"] = {
+                "kernel": "k_clip<float,2> (first clipping pass)", "bound": "fp32", "achieved": achieved,
+                "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32, "traffic": None,
+                "flops_per_cell": fpc,
+                "peak_source": f"nominal: {nsm} SMs x 128 FP32 lanes x 2 x {sm_mhz:.0f} MHz (sampled SM clock)",
+            }
+            nbins = obj.grid()[0] ** 3
+            gbytes = (24 + 24 + 4) * n + 8 * nbins
+            hbm = peaks.get("hbm_gbs", 6800.0)
+            gach = gbytes / (np.mean(grid_ms) / 1e3) / 1e9
+            out["roofline_grid"] = {"kernel": "binning pass (11 launches)", "bound": "hbm", "achieved": gach,
+                                    "peak": hbm, "unit": "GB/s", "frac": gach / hbm,
+                                    "algorithmic_bytes": gbytes, "peak_source": src}
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(args, ws, rank):
+    """The reference's own CPU path is Rust (no toolchain here) and its clipper
+    is unfinished, so the oracle (a C restatement of the reference algorithm)
+    runs with every host thread on a bounded sample of the same workload."""
+    if rank != 0:
+        return
+    pts, batched = make_points(args.workload)
+    vals = []
+    desc = ""
+    for _ in range(args.warmup):
+        cpu_baseline(pts, batched, min(args.cpu_seconds, 5.0))
+    for _ in range(args.steps):
+        rate, _, _, desc = cpu_baseline(pts, batched, args.cpu_seconds)
+        vals.append(rate)
+    rate = float(np.mean(vals))
+    n = len(pts)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "cells/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": n / rate * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload]["desc"], "cells": n, "precision": "FP64 (CPU oracle)"},
+        "cpu_baseline": {"value": rate, "unit": "cells/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": rate, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=list(WORKLOADS), default="uniform16m")
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    import __graft_entry__
+
+    __graft_entry__.build()
+    run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

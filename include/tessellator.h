@@ -1,0 +1,246 @@
+/*
+ * tessellator.h -- C ABI of the GB300 (sm_103a) Voronoi cell library
+ * (libtessgpu.so).  It is the drop-in for the public API of
+ * mcomstock/the-tessellator, src/interface.rs (Diagram, Cell, VoronoiFace).
+ * Each declaration names the reference item it replaces.
+ *
+ * Conventions
+ *  - Every call returns tess_status (0 = TESS_OK).  Nothing aborts or
+ *    throws across the ABI; tess_last_error() returns the message of the
+ *    calling thread's last failure.
+ *  - Point indices are the caller's original indices (0 .. n-1), both for
+ *    cells and for the neighbour ids that faces report
+ *    (interface.rs:329, "original_indices[point_index]").
+ *  - Faces of the container box report negative neighbour ids:
+ *      -1 x_min, -2 x_max, -3 y_min, -4 y_max, -5 z_min, -6 z_max.
+ *    (The reference leaves them as Face { point_index: None },
+ *    polyhedron.rs:300-303, and panics on them in compute_neighbors.)
+ *  - A cell's faces are returned sorted by neighbour id.
+ *  - Vertices are returned relative to the cell's site, as the reference
+ *    leaves its polyhedron translated by -position (interface.rs:266).
+ *  - Output buffers are caller-owned: pass a capacity; when it is too small
+ *    the call returns TESS_E_CAPACITY and still writes the needed count.
+ *  - A handle may be read from several threads at once; create, compute and
+ *    destroy need exclusive access.
+ *  - Every computation runs on the GPU.  There is no CPU fallback: without a
+ *    usable CUDA device the calls return TESS_E_CUDA.
+ */
+#ifndef TESSELLATOR_H
+#define TESSELLATOR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    TESS_OK = 0,
+    TESS_E_INVALID = 1,   /* bad argument (null pointer, n == 0, NaN input, bad index) */
+    TESS_E_CUDA = 2,      /* CUDA runtime error (no device, launch failure)           */
+    TESS_E_CAPACITY = 3,  /* caller buffer too small; the needed size was written     */
+    TESS_E_OVERFLOW = 4,  /* a cell exceeded the largest vertex/face capacity          */
+    TESS_E_STATE = 5,     /* results requested before tess_diagram_compute_all         */
+    TESS_E_NOMEM = 6,     /* device or host allocation failed                          */
+    TESS_E_LIMIT = 7      /* an iteration cap or wait limit was reached                */
+} tess_status;
+
+typedef enum {
+    /* Plain FP64 clipping: the reference's arithmetic type (float.rs:78). */
+    TESS_PRECISION_FP64 = 0,
+    /* FP32 clipping; a cell whose plane-side test lands inside the guard
+     * band, or whose FP32 vertices fail the FP64 check, is re-run in FP64.
+     * Volumes and areas are accumulated in FP64. */
+    TESS_PRECISION_FP32_GUARD = 1
+} tess_precision;
+
+/* Flags for tess_config.flags */
+#define TESS_FLAG_TIMING 1u   /* record per-pass device times (tess_stats) */
+
+typedef struct {
+    /* Guard band of the FP32 form, relative to the current cell radius. */
+    double guard_rel;
+    /* Largest allowed |FP32 vertex - FP64 vertex| / cell radius before a
+     * cell is re-run in FP64. */
+    double verify_rel;
+    /* Points per bin; the reference's cell_density() is 1.25 (celery.rs:185-188). */
+    double bin_density;
+    /* Extent of the precomputed shell table, in bins of gap (>= 1). */
+    int32_t table_gaps;
+    /* Warps per block of the clipping kernel (1..32). */
+    int32_t warps_per_block;
+    /* Vertex slots per lane of the first clipping pass (2, 4 or 8):
+     * capacity = 32 x slots.  Overflowing cells re-run at the next size. */
+    int32_t slots_per_lane;
+    /* CUDA device ordinal. */
+    int32_t device;
+    /* cudaStream_t to run on; NULL: the library's own stream. */
+    void* stream;
+    uint32_t flags;
+} tess_config;
+
+/* Work and timing figures of the last tess_diagram_compute_all. */
+typedef struct {
+    uint64_t cells;             /* cells computed                                  */
+    uint64_t faces;             /* faces over all cells                            */
+    uint64_t rerun_fp64;        /* FP32 cells re-run in FP64 (guard band / check)  */
+    uint64_t rerun_capacity;    /* cells re-run at a larger vertex capacity        */
+    uint64_t failed;            /* cells with an error status                      */
+    uint64_t table_entries;     /* shell-table entries (all diagrams)              */
+    double ms_grid;             /* binning pass (bounds, histogram, scan, scatter) */
+    double ms_clip;             /* first clipping pass                             */
+    double ms_rerun;            /* re-run passes                                   */
+    double ms_csr;              /* CSR compaction                                  */
+    uint64_t launches;          /* kernels launched by this handle so far          */
+} tess_stats;
+
+void tess_config_default(tess_config* cfg);
+/* Message of the calling thread's last failed call ("" if none). Returns its length. */
+size_t tess_last_error(char* buf, size_t cap);
+/* Library version string. */
+const char* tess_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Diagram                                                                    */
+/* ------------------------------------------------------------------------ */
+typedef struct tess_diagram tess_diagram;
+
+/* Replaces Diagram::add_particle_with_group x n + Diagram::initialize
+ * (interface.rs:52-84; both private in the reference, so it has no public
+ * constructor) and Celery::new (celery.rs:231-250).
+ *   xyz     host, n x 3 doubles (AoS)
+ *   groups  host, n group ids (interface.rs:43), or NULL (all 0)
+ *   lo, hi  the container box (the Polyhedron a caller hands to
+ *           get_cell_at_index, interface.rs:186-191), or both NULL: the
+ *           Diagram bounding box, which starts at the origin and grows to
+ *           contain the points (interface.rs:53-54, vector3.rs:263-288).
+ * The points are binned on the GPU (celery.rs:253-414). */
+tess_status tess_diagram_create(const double* xyz, size_t n, const uint32_t* groups,
+                                const double lo[3], const double hi[3],
+                                const tess_config* cfg, tess_diagram** out);
+/* Same, with xyz (n x 3 doubles) already in device memory. */
+tess_status tess_diagram_create_device(const double* d_xyz, size_t n, const uint32_t* groups,
+                                       const double lo[3], const double hi[3],
+                                       const tess_config* cfg, tess_diagram** out);
+/* Re-bin the points currently held (from device memory, no host copy). */
+tess_status tess_diagram_rebuild(tess_diagram* d);
+/* Replace the n points (same count) and re-bin: the points of a Diagram
+ * changed, followed by Celery::reset (celery.rs:253-266).  on_device != 0:
+ * xyz is a device pointer. */
+tess_status tess_diagram_update_points(tess_diagram* d, const double* xyz, int on_device);
+/* The Celery's public fields (celery.rs:196-217) after binning: cells[n]
+ * (bin of each point), sorted_indices[n] (points in bin order, ascending
+ * index within a bin) and delimiters[cpd^3 + 1].  Host buffers; any may be
+ * NULL. */
+tess_status tess_diagram_celery(const tess_diagram* d, uint32_t* cells, uint32_t* sorted_indices,
+                                uint32_t* delimiters);
+tess_status tess_diagram_destroy(tess_diagram* d);
+
+/* Bulk Diagram::get_cell_at_index(i, box, radius, group) +
+ * Cell::compute_voronoi_cell() for every i (interface.rs:186-208, 257-313).
+ *   search_radius  < 0: exact cells (the reference's expand_all_no_radius,
+ *                  celery.rs:971, ended by a security-radius test);
+ *                  >= 0: Some(radius): only bins whose squared gap distance
+ *                  is <= radius are searched, as expand_all_in_radius does
+ *                  (celery.rs:1023-1036).
+ *   target_group   < 0: None; else only points of that group cut
+ *                  (interface.rs:280-297). */
+tess_status tess_diagram_compute_all(tess_diagram* d, tess_precision precision,
+                                     double search_radius, int64_t target_group);
+tess_status tess_diagram_stats(const tess_diagram* d, tess_stats* out);
+/* Grid figures: cells_per_dimension (celery.rs:159) and the tight point bounds
+ * (celery.rs:81-125) as {xmin, xmax, ymin, ymax, zmin, zmax}. */
+tess_status tess_diagram_grid(const tess_diagram* d, int64_t* cpd, double bounds[6]);
+
+/* ---- per-cell queries (after compute_all) ---- */
+/* Cell::compute_volume (interface.rs:337-339, polyhedron.rs:838-855). */
+tess_status tess_cell_volume(const tess_diagram* d, size_t i, double* volume);
+/* Cell::compute_neighbors (interface.rs:342-344, polyhedron.rs:871-881). */
+tess_status tess_cell_neighbors(const tess_diagram* d, size_t i, int32_t* nbr, size_t cap,
+                                size_t* count);
+/* Cell::compute_faces + VoronoiFace::compute_neighbor / compute_area
+ * (interface.rs:373-384, 408-416). */
+tess_status tess_cell_faces(const tess_diagram* d, size_t i, int32_t* nbr, double* area,
+                            size_t cap, size_t* count);
+/* Cell::compute_vertices (interface.rs:368-370, polyhedron.rs:885-893):
+ * site-relative xyz, 3 doubles per vertex.  Recomputes the cell on the GPU
+ * with the last compute_all settings. */
+tess_status tess_cell_vertices(tess_diagram* d, size_t i, double* xyz, size_t cap,
+                               size_t* count);
+/* VoronoiFace::compute_vertices (interface.rs:403-405, polyhedron.rs:897-919):
+ * vertex cycle of face `face` (index into the sorted face list),
+ * counter-clockwise seen from outside the cell. */
+tess_status tess_cell_face_vertices(tess_diagram* d, size_t i, size_t face, double* xyz,
+                                    size_t cap, size_t* count);
+/* Cell::original_index (interface.rs:387-389): identity under the
+ * original-index convention. */
+tess_status tess_cell_original_index(const tess_diagram* d, size_t i, size_t* original);
+
+/* One cell computed on its own, with its full geometry. */
+#define TESS_MAX_CELL_VERTICES 255
+#define TESS_MAX_CELL_FACES 254
+typedef struct {
+    double volume;                       /* polyhedron.rs:838-855                    */
+    int32_t nvertices;                   /* polyhedron.rs:885-893                    */
+    int32_t nfaces;
+    double vertices[3 * 256];            /* site-relative xyz                        */
+    int32_t face_neighbor[256];          /* sorted; walls -1 .. -6                   */
+    double face_area[256];               /* interface.rs:408-410                     */
+    int32_t face_offset[257];            /* face f: face_vertex[face_offset[f] ..]   */
+    int32_t face_vertex[3 * 256];        /* vertex indices, CCW seen from outside    */
+} tess_cell_geometry;
+
+/* Diagram::get_cell_at_index(i, polyhedron, search_radius, target_group) +
+ * Cell::compute_voronoi_cell (interface.rs:186-208, 257-313) for one cell.
+ * lo/hi: the container box for this cell (the Polyhedron argument), or both
+ * NULL for the diagram's box. */
+tess_status tess_cell_compute(tess_diagram* d, size_t i, tess_precision precision, double search_radius,
+                              int64_t target_group, const double lo[3], const double hi[3],
+                              tess_cell_geometry* out);
+/* Diagram::get_cell_at_particle + compute_voronoi_cell (interface.rs:211-232):
+ * the cell of a point that is not in the diagram (no self exclusion). */
+tess_status tess_cell_compute_at(tess_diagram* d, const double p[3], tess_precision precision,
+                                 double search_radius, int64_t target_group, const double lo[3],
+                                 const double hi[3], tess_cell_geometry* out);
+
+/* ---- bulk results ---- */
+/* All volumes, host buffer of n doubles. */
+tess_status tess_volumes(tess_diagram* d, double* volumes);
+/* CSR of all faces in original cell order: offs[n+1], nbr[total], area[total]
+ * (host buffers).  Any of nbr/area may be NULL; cap is their capacity. */
+tess_status tess_neighbors_csr(tess_diagram* d, uint64_t* offs, int32_t* nbr, double* area,
+                               size_t cap, size_t* total);
+/* Device pointers to the same results (valid until the next compute or
+ * destroy): volumes[n], offs[n+1], nbr[total], area[total]. */
+tess_status tess_results_device(tess_diagram* d, const double** volumes, const uint64_t** offs,
+                                const int32_t** nbr, const double** area, size_t* total);
+
+/* ------------------------------------------------------------------------ */
+/* Batch: many independent diagrams, one persistent launch per pass,          */
+/* captured in a CUDA graph (no reference counterpart: the reference builds   */
+/* one Diagram at a time).                                                    */
+/* ------------------------------------------------------------------------ */
+typedef struct tess_batch tess_batch;
+
+/*   pt_offsets  ndiag+1 offsets into xyz (host)
+ *   xyz         host, total x 3 doubles
+ *   boxes       host, ndiag x 6 doubles {xlo, ylo, zlo, xhi, yhi, zhi} */
+tess_status tess_batch_create(size_t ndiag, const uint64_t* pt_offsets, const double* xyz,
+                              const double* boxes, const tess_config* cfg, tess_batch** out);
+/* Bin and clip every diagram.  The sequence of launches is captured in a CUDA
+ * graph on first use and replayed afterwards. */
+tess_status tess_batch_compute(tess_batch* b, tess_precision precision);
+tess_status tess_batch_stats(const tess_batch* b, tess_stats* out);
+/* Volumes of all points (concatenated order), host buffer. */
+tess_status tess_batch_volumes(tess_batch* b, double* volumes);
+/* CSR over all points (concatenated order); neighbour ids are indices local
+ * to each diagram. */
+tess_status tess_batch_neighbors_csr(tess_batch* b, uint64_t* offs, int32_t* nbr, double* area,
+                                     size_t cap, size_t* total);
+tess_status tess_batch_destroy(tess_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

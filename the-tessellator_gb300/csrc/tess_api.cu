@@ -1,0 +1,1041 @@
+// tess_api.cu -- host driver and C ABI of libtessgpu.so (declared in
+// include/tessellator.h).  Owns the device buffers of a set of diagrams,
+// sequences the binning pass and the clipping passes on one CUDA stream, and
+// serves the per-cell and bulk queries of the reference's interface.rs API.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tess_internal.cuh"
+#include "tessellator.h"
+
+using namespace tess;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+tess_status fail(tess_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+#define CU(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(e_ == cudaErrorMemoryAllocation ? TESS_E_NOMEM : TESS_E_CUDA, "%s: %s (%s:%d)", \
+                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                       \
+    } while (0)
+
+#define TRY(call)                                                                                  \
+    do {                                                                                           \
+        tess_status s_ = (call);                                                                   \
+        if (s_ != TESS_OK) return s_;                                                              \
+    } while (0)
+
+template <typename T>
+tess_status dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    CU(cudaMalloc((void**)p, sizeof(T) * count));
+    return TESS_OK;
+}
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+// cells_per_dimension = (n / density).cbrt() as usize + 1 (celery.rs:159-160),
+// with the host's libm cbrt.
+int64_t cells_per_dim(uint64_t n, double density) {
+    const double v = std::cbrt((double)n / density);
+    if (!(v > 0.0)) return 1;
+    return (int64_t)v + 1;
+}
+
+enum { L_FP64 = 0, L_CAP1 = 1, L_CAP2 = 2, L_CAP64A = 3, L_CAP64B = 4, L_COUNT = 5, L_FAIL = 10 };
+// Kernels launched by one binning pass (launch_grid_build).
+constexpr uint64_t kGridLaunches = 11;
+
+struct Engine {
+    tess_config cfg{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    size_t ndiag = 0;
+    uint32_t total = 0;
+    uint64_t total_bins = 0;
+    uint64_t table_total = 0;
+    uint32_t nchunks = 0;
+    bool has_groups = false;
+    std::vector<DiagDesc> hdesc;
+    // device
+    double* d_xyz = nullptr;
+    uint32_t* d_groups = nullptr;
+    DiagDesc* d_desc = nullptr;
+    uint32_t* d_chunk_diag = nullptr;
+    uint32_t* d_chunk_start = nullptr;
+    unsigned long long* d_bounds = nullptr;
+    uint32_t* d_bin = nullptr;
+    uint32_t* d_rank = nullptr;
+    uint32_t* d_delims = nullptr;
+    uint32_t* d_scan_tmp = nullptr;
+    uint32_t* d_sorted = nullptr;
+    uint32_t* d_inv = nullptr;
+    double* d_spx = nullptr;
+    double* d_spy = nullptr;
+    double* d_spz = nullptr;
+    uint32_t* d_sgroup = nullptr;
+    TabEntry* d_table = nullptr;
+    int* d_err = nullptr;
+    // results
+    double* d_vol = nullptr;
+    uint32_t* d_nface = nullptr;
+    uint64_t* d_fstart = nullptr;
+    uint8_t* d_status = nullptr;
+    int32_t* d_fnbr = nullptr;
+    double* d_farea = nullptr;
+    uint64_t face_cap = 0;
+    unsigned long long* d_fcursor = nullptr;
+    uint32_t* d_list[L_COUNT] = {};
+    unsigned* d_counters = nullptr;   // [0..15] cursors, [16..31] list counts
+    uint64_t* d_offs = nullptr;
+    int32_t* d_cnbr = nullptr;
+    double* d_carea = nullptr;
+    uint64_t csr_cap = 0;
+    uint64_t* d_csr_tmp = nullptr;
+    GeoOut* d_geo = nullptr;
+    uint32_t* d_one = nullptr;
+    // state
+    bool built = false;
+    bool computed = false;
+    bool csr_valid = false;
+    uint64_t csr_total = 0;
+    int last_precision = TESS_PRECISION_FP64;
+    double last_radius = -1.0;
+    int64_t last_group = -1;
+    tess_stats stats{};
+    uint64_t launches = 0;    // kernels launched so far (all passes)
+    cudaGraphExec_t graph = nullptr;
+    int graph_precision = -1;
+    int blocks_cache[2][4] = {};
+
+    ~Engine() { release(); }
+
+    void release() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        dfree(d_xyz); dfree(d_groups); dfree(d_desc); dfree(d_chunk_diag); dfree(d_chunk_start);
+        dfree(d_bounds); dfree(d_bin); dfree(d_rank); dfree(d_delims); dfree(d_scan_tmp);
+        dfree(d_sorted); dfree(d_inv); dfree(d_spx); dfree(d_spy); dfree(d_spz); dfree(d_sgroup);
+        dfree(d_table); dfree(d_err); dfree(d_vol); dfree(d_nface); dfree(d_fstart); dfree(d_status);
+        dfree(d_fnbr); dfree(d_farea); dfree(d_fcursor);
+        for (auto& l : d_list) dfree(l);
+        dfree(d_counters); dfree(d_offs); dfree(d_cnbr); dfree(d_carea); dfree(d_csr_tmp);
+        dfree(d_geo); dfree(d_one);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+
+    int blocks(int precision, int slots) {
+        const int si = slots <= 2 ? 0 : (slots <= 4 ? 1 : 2);
+        int& b = blocks_cache[precision][si];
+        if (!b) {
+            const int wpb = wpb_for(precision, slots);
+            b = clip_blocks_for(precision, slots, wpb, device);
+        }
+        return b;
+    }
+    int wpb_for(int precision, int slots) const {
+        int w = cfg.warps_per_block;
+        if (slots >= 8) w = std::min(w, precision == 1 ? 4 : 2);
+        else if (slots >= 4) w = std::min(w, 4);
+        return std::max(1, w);
+    }
+};
+
+void fill_defaults(tess_config* c) {
+    c->guard_rel = 2e-5;
+    c->verify_rel = 1e-5;
+    c->bin_density = 1.25;
+    c->table_gaps = 8;
+    c->warps_per_block = 8;
+    c->slots_per_lane = 2;
+    c->device = 0;
+    c->stream = nullptr;
+    c->flags = 0;
+}
+
+tess_status check_config(const tess_config& c) {
+    if (!(c.bin_density > 0.0) || !std::isfinite(c.bin_density)) return fail(TESS_E_INVALID, "bin_density must be > 0");
+    if (c.table_gaps < 1 || c.table_gaps > 8) return fail(TESS_E_INVALID, "table_gaps must be in [1, 8]");
+    if (c.warps_per_block < 1 || c.warps_per_block > 32) return fail(TESS_E_INVALID, "warps_per_block must be in [1, 32]");
+    if (c.slots_per_lane != 2 && c.slots_per_lane != 4 && c.slots_per_lane != 8)
+        return fail(TESS_E_INVALID, "slots_per_lane must be 2, 4 or 8");
+    if (!(c.guard_rel >= 0.0) || !(c.guard_rel < 1.0)) return fail(TESS_E_INVALID, "guard_rel must be in [0, 1)");
+    return TESS_OK;
+}
+
+// Allocate everything for `diags` (pt_base/n/box set) and copy the points.
+tess_status engine_init(Engine& E, const tess_config* cfg, std::vector<DiagDesc>& diags, const double* xyz,
+                        bool xyz_on_device, const uint32_t* groups) {
+    if (cfg) E.cfg = *cfg;
+    else fill_defaults(&E.cfg);
+    TRY(check_config(E.cfg));
+    E.device = E.cfg.device;
+    int ndev = 0;
+    cudaError_t ce = cudaGetDeviceCount(&ndev);
+    if (ce != cudaSuccess || ndev == 0)
+        return fail(TESS_E_CUDA, "no CUDA device available (%s)", cudaGetErrorString(ce));
+    if (E.device < 0 || E.device >= ndev) return fail(TESS_E_INVALID, "device %d out of range", E.device);
+    CU(cudaSetDevice(E.device));
+    if (E.cfg.stream) {
+        E.stream = (cudaStream_t)E.cfg.stream;
+        E.own_stream = false;
+    } else {
+        CU(cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking));
+        E.own_stream = true;
+    }
+    E.ndiag = diags.size();
+    uint64_t total = 0, bins = 0, tab = 0;
+    std::vector<uint32_t> cdiag, cstart;
+    for (size_t d = 0; d < diags.size(); ++d) {
+        DiagDesc& D = diags[d];
+        const int64_t cpd = cells_per_dim(D.n, E.cfg.bin_density);
+        if (cpd > 1625) return fail(TESS_E_INVALID, "diagram %zu: %u points give %lld bins per axis (max 1625)",
+                                    d, D.n, (long long)cpd);
+        D.cpd = (int32_t)cpd;
+        D.bin_base = bins;
+        bins += (uint64_t)cpd * cpd * cpd;
+        int c = E.cfg.table_gaps + 1;
+        if (c > cpd - 1) c = (int)cpd - 1;
+        if (c < 0) c = 0;
+        const uint64_t cube = (uint64_t)(2 * c + 1) * (2 * c + 1) * (2 * c + 1);
+        D.tab_cap = (uint32_t)std::min<uint64_t>(cube, (uint64_t)kMaxTable);
+        D.tab_base = tab;
+        tab += D.tab_cap;
+        D.tab_len = 0;
+        for (uint32_t s = 0; s < D.n; s += kChunk) {
+            cdiag.push_back((uint32_t)d);
+            cstart.push_back(D.pt_base + s);
+        }
+        total += D.n;
+    }
+    if (total >= 0xFFFFFFF0ull) return fail(TESS_E_INVALID, "too many points (%llu)", (unsigned long long)total);
+    if (bins + 1 >= 0xFFFFFFF0ull) return fail(TESS_E_INVALID, "too many bins (%llu)", (unsigned long long)bins);
+    E.total = (uint32_t)total;
+    E.total_bins = bins;
+    E.table_total = tab;
+    E.nchunks = (uint32_t)cdiag.size();
+    E.hdesc = diags;
+    E.has_groups = groups != nullptr;
+    const size_t n = E.total;
+    TRY(dalloc(&E.d_xyz, 3 * n));
+    if (xyz_on_device) CU(cudaMemcpyAsync(E.d_xyz, xyz, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, E.stream));
+    else CU(cudaMemcpyAsync(E.d_xyz, xyz, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, E.stream));
+    if (groups) {
+        TRY(dalloc(&E.d_groups, n));
+        CU(cudaMemcpyAsync(E.d_groups, groups, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, E.stream));
+        TRY(dalloc(&E.d_sgroup, n));
+    }
+    TRY(dalloc(&E.d_desc, E.ndiag));
+    CU(cudaMemcpyAsync(E.d_desc, diags.data(), sizeof(DiagDesc) * E.ndiag, cudaMemcpyHostToDevice, E.stream));
+    TRY(dalloc(&E.d_chunk_diag, E.nchunks));
+    TRY(dalloc(&E.d_chunk_start, E.nchunks));
+    CU(cudaMemcpyAsync(E.d_chunk_diag, cdiag.data(), sizeof(uint32_t) * E.nchunks, cudaMemcpyHostToDevice, E.stream));
+    CU(cudaMemcpyAsync(E.d_chunk_start, cstart.data(), sizeof(uint32_t) * E.nchunks, cudaMemcpyHostToDevice, E.stream));
+    TRY(dalloc(&E.d_bounds, 6 * E.ndiag));
+    TRY(dalloc(&E.d_bin, n));
+    TRY(dalloc(&E.d_rank, n));
+    TRY(dalloc(&E.d_delims, E.total_bins + 1));
+    TRY(dalloc(&E.d_scan_tmp, scan_tmp_words(E.total_bins + 1)));
+    TRY(dalloc(&E.d_sorted, n));
+    TRY(dalloc(&E.d_inv, n));
+    TRY(dalloc(&E.d_spx, n));
+    TRY(dalloc(&E.d_spy, n));
+    TRY(dalloc(&E.d_spz, n));
+    TRY(dalloc(&E.d_table, E.table_total));
+    TRY(dalloc(&E.d_err, 1));
+    TRY(dalloc(&E.d_vol, n));
+    TRY(dalloc(&E.d_nface, n));
+    TRY(dalloc(&E.d_fstart, n));
+    TRY(dalloc(&E.d_status, n));
+    E.face_cap = (uint64_t)n * 20 + 4096;
+    TRY(dalloc(&E.d_fnbr, E.face_cap));
+    TRY(dalloc(&E.d_farea, E.face_cap));
+    TRY(dalloc(&E.d_fcursor, 1));
+    for (auto& l : E.d_list) TRY(dalloc(&l, n));
+    TRY(dalloc(&E.d_counters, 32));
+    TRY(dalloc(&E.d_offs, n + 1));
+    TRY(dalloc(&E.d_csr_tmp, csr_tmp_words(E.total)));
+    TRY(dalloc(&E.d_geo, 1));
+    TRY(dalloc(&E.d_one, 1));
+    return TESS_OK;
+}
+
+GridBuffers grid_buffers(Engine& E) {
+    GridBuffers g{};
+    g.xyz = E.d_xyz;
+    g.groups = E.d_groups;
+    g.diags = E.d_desc;
+    g.ndiag = (int)E.ndiag;
+    g.total = E.total;
+    g.total_bins = E.total_bins;
+    g.chunk_diag = E.d_chunk_diag;
+    g.chunk_start = E.d_chunk_start;
+    g.nchunks = E.nchunks;
+    g.bounds = E.d_bounds;
+    g.bin = E.d_bin;
+    g.rank = E.d_rank;
+    g.delims = E.d_delims;
+    g.scan_tmp = E.d_scan_tmp;
+    g.sorted = E.d_sorted;
+    g.inv = E.d_inv;
+    g.spx = E.d_spx;
+    g.spy = E.d_spy;
+    g.spz = E.d_spz;
+    g.sgroup = E.d_sgroup;
+    g.table = E.d_table;
+    g.table_gaps = E.cfg.table_gaps;
+    g.error_flag = E.d_err;
+    return g;
+}
+
+tess_status engine_build(Engine& E, bool check) {
+    CU(cudaSetDevice(E.device));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
+    if (timing) {
+        CU(cudaEventCreate(&e0));
+        CU(cudaEventCreate(&e1));
+        CU(cudaEventRecord(e0, E.stream));
+    }
+    CU(launch_grid_build(grid_buffers(E), E.stream));
+    E.launches += kGridLaunches;
+    if (timing) CU(cudaEventRecord(e1, E.stream));
+    if (check) {
+        int err = 0;
+        CU(cudaMemcpyAsync(&err, E.d_err, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
+        CU(cudaStreamSynchronize(E.stream));
+        if (err == 1) return fail(TESS_E_INVALID, "input coordinates must be finite");
+        if (err == 2) return fail(TESS_E_CUDA, "shell table exceeded its capacity");
+    }
+    if (timing) {
+        CU(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        E.stats.ms_grid = ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    E.built = true;
+    E.computed = false;
+    E.csr_valid = false;
+    return TESS_OK;
+}
+
+ClipParams base_params(Engine& E) {
+    ClipParams p{};
+    p.diags = E.d_desc;
+    p.ndiag = (int)E.ndiag;
+    p.spx = E.d_spx;
+    p.spy = E.d_spy;
+    p.spz = E.d_spz;
+    p.sorted = E.d_sorted;
+    p.delims = E.d_delims;
+    p.sgroup = E.d_sgroup;
+    p.table = E.d_table;
+    p.total = E.total;
+    p.vol = E.d_vol;
+    p.nface = E.d_nface;
+    p.fstart = E.d_fstart;
+    p.status = E.d_status;
+    p.face_nbr = E.d_fnbr;
+    p.face_area = E.d_farea;
+    p.face_cursor = E.d_fcursor;
+    p.face_cap = E.face_cap;
+    p.guard_rel = (float)E.cfg.guard_rel;
+    p.verify_rel = (float)E.cfg.verify_rel;
+    return p;
+}
+
+// The fixed launch sequence of one compute (no host synchronisation):
+// first pass, capacity re-runs, FP64 re-runs.  Counters: cursor c at
+// d_counters[c], list counts at d_counters[16 + list].
+tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t group, bool timing,
+                           cudaEvent_t* ev) {
+    unsigned* cur = E.d_counters;
+    unsigned* cnt = E.d_counters + 16;
+    CU(cudaMemsetAsync(E.d_counters, 0, sizeof(unsigned) * 32, E.stream));
+    CU(cudaMemsetAsync(E.d_fcursor, 0, sizeof(unsigned long long), E.stream));
+    ClipParams base = base_params(E);
+    base.search_radius = radius;
+    base.target_group = group;
+    const int s0 = E.cfg.slots_per_lane;
+    int cursor = 0;
+    auto pass = [&](int prec, int slots, const uint32_t* work, const unsigned* wcount, uint32_t* l64,
+                    unsigned* c64, uint32_t* lcap, unsigned* ccap) -> tess_status {
+        ClipParams p = base;
+        p.work = work;
+        p.work_count = wcount;
+        p.cursor = cur + cursor++;
+        p.list_fp64 = l64;
+        p.list_fp64_count = c64;
+        p.list_cap = lcap;
+        p.list_cap_count = ccap;
+        p.fail_count = cnt + L_FAIL;
+        CU(launch_clip(p, prec, slots, E.wpb_for(prec, slots), E.blocks(prec, slots), E.stream));
+        E.launches += 1;
+        return TESS_OK;
+    };
+    if (timing) CU(cudaEventRecord(ev[0], E.stream));
+    if (precision == TESS_PRECISION_FP32_GUARD) {
+        // FP32: s0 -> larger capacities; guard / degenerate cells -> FP64 list
+        const bool two = s0 < 4, one = s0 < 8;
+        TRY(pass(1, s0, nullptr, nullptr, E.d_list[L_FP64], cnt + L_FP64, one ? E.d_list[L_CAP1] : nullptr,
+                 cnt + L_CAP1));
+        if (timing) CU(cudaEventRecord(ev[1], E.stream));
+        if (one) {
+            const int s1 = two ? 4 : 8;
+            TRY(pass(1, s1, E.d_list[L_CAP1], cnt + L_CAP1, E.d_list[L_FP64], cnt + L_FP64,
+                     two ? E.d_list[L_CAP2] : nullptr, cnt + L_CAP2));
+            if (two)
+                TRY(pass(1, 8, E.d_list[L_CAP2], cnt + L_CAP2, E.d_list[L_FP64], cnt + L_FP64, nullptr, nullptr));
+        }
+        TRY(pass(0, 2, E.d_list[L_FP64], cnt + L_FP64, nullptr, nullptr, E.d_list[L_CAP64A], cnt + L_CAP64A));
+        TRY(pass(0, 4, E.d_list[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, E.d_list[L_CAP64B], cnt + L_CAP64B));
+        TRY(pass(0, 8, E.d_list[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
+    } else {
+        const bool two = s0 < 4, one = s0 < 8;
+        TRY(pass(0, s0, nullptr, nullptr, nullptr, nullptr, one ? E.d_list[L_CAP64A] : nullptr, cnt + L_CAP64A));
+        if (timing) CU(cudaEventRecord(ev[1], E.stream));
+        if (one) {
+            const int s1 = two ? 4 : 8;
+            TRY(pass(0, s1, E.d_list[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, two ? E.d_list[L_CAP64B] : nullptr,
+                     cnt + L_CAP64B));
+            if (two) TRY(pass(0, 8, E.d_list[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
+        }
+    }
+    if (timing) CU(cudaEventRecord(ev[2], E.stream));
+    return TESS_OK;
+}
+
+tess_status engine_compute(Engine& E, int precision, double radius, int64_t group) {
+    if (!E.built) return fail(TESS_E_STATE, "diagram is not built");
+    if (precision != TESS_PRECISION_FP64 && precision != TESS_PRECISION_FP32_GUARD)
+        return fail(TESS_E_INVALID, "unknown precision %d", precision);
+    if (std::isnan(radius)) return fail(TESS_E_INVALID, "search_radius is NaN");
+    CU(cudaSetDevice(E.device));
+    const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
+    cudaEvent_t ev[3] = {};
+    if (timing)
+        for (auto& e : ev) CU(cudaEventCreate(&e));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        TRY(enqueue_passes(E, precision, radius, group, timing, ev));
+        unsigned long long used = 0;
+        unsigned counts[16];
+        CU(cudaMemcpyAsync(&used, E.d_fcursor, sizeof(used), cudaMemcpyDeviceToHost, E.stream));
+        CU(cudaMemcpyAsync(counts, E.d_counters + 16, sizeof(counts), cudaMemcpyDeviceToHost, E.stream));
+        CU(cudaStreamSynchronize(E.stream));
+        if (used > E.face_cap) {
+            // face pool too small: grow and recompute
+            dfree(E.d_fnbr);
+            dfree(E.d_farea);
+            E.face_cap = std::max<uint64_t>(2 * E.face_cap, used + used / 4 + 4096);
+            TRY(dalloc(&E.d_fnbr, E.face_cap));
+            TRY(dalloc(&E.d_farea, E.face_cap));
+            continue;
+        }
+        E.stats.cells = E.total;
+        E.stats.faces = used;
+        if (precision == TESS_PRECISION_FP32_GUARD) {
+            E.stats.rerun_fp64 = counts[L_FP64];
+            E.stats.rerun_capacity = (uint64_t)counts[L_CAP1] + counts[L_CAP2] + counts[L_CAP64A] + counts[L_CAP64B];
+        } else {
+            E.stats.rerun_fp64 = 0;
+            E.stats.rerun_capacity = (uint64_t)counts[L_CAP64A] + counts[L_CAP64B];
+        }
+        if (E.ndiag == 1) {
+            DiagDesc dd;
+            CU(cudaMemcpy(&dd, E.d_desc, sizeof(DiagDesc), cudaMemcpyDeviceToHost));
+            E.stats.table_entries = dd.tab_len;
+        }
+        if (timing) {
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, ev[0], ev[1]);
+            cudaEventElapsedTime(&b, ev[1], ev[2]);
+            E.stats.ms_clip = a;
+            E.stats.ms_rerun = b;
+            for (auto& e : ev) cudaEventDestroy(e);
+        }
+        E.computed = true;
+        E.csr_valid = false;
+        E.last_precision = precision;
+        E.last_radius = radius;
+        E.last_group = group;
+        const uint64_t failed = counts[L_FAIL];
+        E.stats.failed = failed;
+        if (failed) return fail(TESS_E_OVERFLOW, "%llu cells could not be computed", (unsigned long long)failed);
+        return TESS_OK;
+    }
+    return fail(TESS_E_NOMEM, "face pool could not be sized");
+}
+
+tess_status engine_csr(Engine& E) {
+    if (!E.computed) return fail(TESS_E_STATE, "compute_all has not run");
+    if (E.csr_valid) return TESS_OK;
+    CU(cudaSetDevice(E.device));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
+    if (timing) {
+        CU(cudaEventCreate(&e0));
+        CU(cudaEventCreate(&e1));
+    }
+    // offsets first (to size the outputs), then the gather
+    if (timing) CU(cudaEventRecord(e0, E.stream));
+    CU(launch_csr_offsets(E.d_nface, E.total, E.d_offs, E.d_csr_tmp, E.stream));
+    uint64_t total = 0;
+    CU(cudaMemcpyAsync(&total, E.d_offs + E.total, sizeof(uint64_t), cudaMemcpyDeviceToHost, E.stream));
+    CU(cudaStreamSynchronize(E.stream));
+    if (total > E.csr_cap || !E.d_cnbr) {
+        dfree(E.d_cnbr);
+        dfree(E.d_carea);
+        E.csr_cap = total + total / 8 + 1024;
+        TRY(dalloc(&E.d_cnbr, E.csr_cap));
+        TRY(dalloc(&E.d_carea, E.csr_cap));
+    }
+    CU(launch_csr_gather(E.d_nface, E.d_fstart, E.d_fnbr, E.d_farea, E.total, E.d_offs, E.d_cnbr, E.d_carea,
+                         E.stream));
+    E.launches += 4;
+    if (timing) {
+        CU(cudaEventRecord(e1, E.stream));
+        CU(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        E.stats.ms_csr = ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    E.csr_total = total;
+    E.csr_valid = true;
+    return TESS_OK;
+}
+
+// One cell's full geometry: re-run the cell alone (FP64 re-run if the FP32
+// form declines it) into the GeoOut buffer and copy it back.
+tess_status engine_geo(Engine& E, int precision, uint32_t gs, const double* point, double radius, int64_t group,
+                       const double* lo, const double* hi, GeoOut* out) {
+    CU(cudaSetDevice(E.device));
+    for (int prec : {precision, (int)TESS_PRECISION_FP64}) {
+        ClipParams p = base_params(E);
+        p.search_radius = radius;
+        p.target_group = group;
+        CU(cudaMemcpyAsync(E.d_one, &gs, sizeof(uint32_t), cudaMemcpyHostToDevice, E.stream));
+        CU(cudaMemsetAsync(E.d_counters, 0, sizeof(unsigned) * 32, E.stream));
+        p.work = E.d_one;
+        p.work_count = nullptr;
+        p.total = 1;
+        p.cursor = E.d_counters;
+        p.geo = E.d_geo;
+        if (point) {
+            p.at_point = 1;
+            p.point[0] = point[0];
+            p.point[1] = point[1];
+            p.point[2] = point[2];
+        }
+        if (lo) {
+            p.box_override = 1;
+            for (int a = 0; a < 3; ++a) {
+                p.box[a] = lo[a];
+                p.box[3 + a] = hi[a];
+            }
+        }
+        CU(launch_clip(p, prec == TESS_PRECISION_FP32_GUARD ? 1 : 0, 8, 1, 1, E.stream));
+        CU(cudaMemcpyAsync(out, E.d_geo, sizeof(GeoOut), cudaMemcpyDeviceToHost, E.stream));
+        CU(cudaStreamSynchronize(E.stream));
+        if (out->status == ST_OK) return TESS_OK;
+        if (prec == TESS_PRECISION_FP64) break;
+    }
+    return fail(TESS_E_OVERFLOW, "cell could not be computed (status %d)", out->status);
+}
+
+tess_status validate_box(const double* lo, const double* hi) {
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(lo[a]) || !std::isfinite(hi[a]) || !(lo[a] <= hi[a]))
+            return fail(TESS_E_INVALID, "container box must satisfy lo <= hi (axis %d)", a);
+    return TESS_OK;
+}
+
+}  // namespace
+
+struct tess_diagram {
+    Engine E;
+    uint32_t n = 0;
+};
+struct tess_batch {
+    Engine E;
+};
+
+extern "C" {
+
+void tess_config_default(tess_config* cfg) {
+    if (cfg) fill_defaults(cfg);
+}
+
+size_t tess_last_error(char* buf, size_t cap) {
+    const size_t n = g_last_error.size();
+    if (buf && cap) {
+        const size_t m = std::min(n, cap - 1);
+        memcpy(buf, g_last_error.data(), m);
+        buf[m] = 0;
+    }
+    return n;
+}
+
+const char* tess_version(void) { return "tessellator-gb300 0.1 (sm_103a)"; }
+
+static tess_status create_common(const double* xyz, bool on_device, size_t n, const uint32_t* groups,
+                                 const double lo[3], const double hi[3], const tess_config* cfg,
+                                 tess_diagram** out) {
+    if (!out) return fail(TESS_E_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!xyz) return fail(TESS_E_INVALID, "xyz is NULL");
+    if (n == 0) return fail(TESS_E_INVALID, "a diagram needs at least one point");
+    if ((lo == nullptr) != (hi == nullptr)) return fail(TESS_E_INVALID, "give both lo and hi, or neither");
+    DiagDesc D{};
+    D.pt_base = 0;
+    D.n = (uint32_t)n;
+    if (lo) {
+        TRY(validate_box(lo, hi));
+        for (int a = 0; a < 3; ++a) {
+            D.blo[a] = lo[a];
+            D.bhi[a] = hi[a];
+        }
+    } else {
+        // The Diagram bounding box: starts at the origin and grows to contain
+        // every point (interface.rs:53-54, vector3.rs:263-288).
+        std::vector<double> hx;
+        const double* src = xyz;
+        if (on_device) {
+            hx.resize(3 * n);
+            cudaError_t e = cudaMemcpy(hx.data(), xyz, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return fail(TESS_E_CUDA, "reading device points: %s", cudaGetErrorString(e));
+            src = hx.data();
+        }
+        for (int a = 0; a < 3; ++a) D.blo[a] = D.bhi[a] = 0.0;
+        for (size_t i = 0; i < n; ++i)
+            for (int a = 0; a < 3; ++a) {
+                const double v = src[3 * i + a];
+                if (v < D.blo[a]) D.blo[a] = v;
+                if (v > D.bhi[a]) D.bhi[a] = v;
+            }
+    }
+    tess_diagram* h = new (std::nothrow) tess_diagram();
+    if (!h) return fail(TESS_E_NOMEM, "host allocation failed");
+    h->n = (uint32_t)n;
+    std::vector<DiagDesc> v{D};
+    tess_status st = engine_init(h->E, cfg, v, xyz, on_device, groups);
+    if (st == TESS_OK) st = engine_build(h->E, true);
+    if (st != TESS_OK) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    return TESS_OK;
+}
+
+tess_status tess_diagram_create(const double* xyz, size_t n, const uint32_t* groups, const double lo[3],
+                                const double hi[3], const tess_config* cfg, tess_diagram** out) {
+    return create_common(xyz, false, n, groups, lo, hi, cfg, out);
+}
+
+tess_status tess_diagram_create_device(const double* d_xyz, size_t n, const uint32_t* groups, const double lo[3],
+                                       const double hi[3], const tess_config* cfg, tess_diagram** out) {
+    return create_common(d_xyz, true, n, groups, lo, hi, cfg, out);
+}
+
+tess_status tess_diagram_rebuild(tess_diagram* d) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    return engine_build(d->E, false);
+}
+
+tess_status tess_diagram_destroy(tess_diagram* d) {
+    delete d;
+    return TESS_OK;
+}
+
+tess_status tess_diagram_compute_all(tess_diagram* d, tess_precision precision, double search_radius,
+                                     int64_t target_group) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    return engine_compute(d->E, (int)precision, search_radius, target_group);
+}
+
+tess_status tess_diagram_stats(const tess_diagram* d, tess_stats* out) {
+    if (!d || !out) return fail(TESS_E_INVALID, "NULL argument");
+    *out = d->E.stats;
+    out->launches = d->E.launches;
+    return TESS_OK;
+}
+
+tess_status tess_diagram_update_points(tess_diagram* d, const double* xyz, int on_device) {
+    if (!d || !xyz) return fail(TESS_E_INVALID, "NULL argument");
+    Engine& E = d->E;
+    CU(cudaSetDevice(E.device));
+    CU(cudaMemcpyAsync(E.d_xyz, xyz, sizeof(double) * 3 * (size_t)E.total,
+                       on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, E.stream));
+    return engine_build(E, true);
+}
+
+tess_status tess_diagram_celery(const tess_diagram* d, uint32_t* cells, uint32_t* sorted_indices,
+                                uint32_t* delimiters) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    const Engine& E = d->E;
+    CU(cudaSetDevice(E.device));
+    if (cells) CU(cudaMemcpy(cells, E.d_bin, sizeof(uint32_t) * E.total, cudaMemcpyDeviceToHost));
+    if (sorted_indices) CU(cudaMemcpy(sorted_indices, E.d_sorted, sizeof(uint32_t) * E.total, cudaMemcpyDeviceToHost));
+    if (delimiters)
+        CU(cudaMemcpy(delimiters, E.d_delims, sizeof(uint32_t) * (E.total_bins + 1), cudaMemcpyDeviceToHost));
+    return TESS_OK;
+}
+
+tess_status tess_diagram_grid(const tess_diagram* d, int64_t* cpd, double bounds[6]) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    DiagDesc D;
+    CU(cudaSetDevice(d->E.device));
+    CU(cudaMemcpy(&D, d->E.d_desc, sizeof(D), cudaMemcpyDeviceToHost));
+    if (cpd) *cpd = D.cpd;
+    if (bounds)
+        for (int a = 0; a < 3; ++a) {
+            bounds[2 * a] = D.glo[a];
+            bounds[2 * a + 1] = D.ghi[a];
+        }
+    return TESS_OK;
+}
+
+static tess_status cell_check(const tess_diagram* d, size_t i) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    if (i >= d->n) return fail(TESS_E_INVALID, "cell index %zu out of range (n = %u)", i, d->n);
+    if (!d->E.computed) return fail(TESS_E_STATE, "compute_all has not run");
+    return TESS_OK;
+}
+
+tess_status tess_cell_volume(const tess_diagram* d, size_t i, double* volume) {
+    TRY(cell_check(d, i));
+    if (!volume) return fail(TESS_E_INVALID, "volume is NULL");
+    CU(cudaSetDevice(d->E.device));
+    CU(cudaMemcpy(volume, d->E.d_vol + i, sizeof(double), cudaMemcpyDeviceToHost));
+    return TESS_OK;
+}
+
+tess_status tess_cell_faces(const tess_diagram* d, size_t i, int32_t* nbr, double* area, size_t cap,
+                            size_t* count) {
+    TRY(cell_check(d, i));
+    CU(cudaSetDevice(d->E.device));
+    uint32_t nf = 0;
+    uint64_t fs = 0;
+    CU(cudaMemcpy(&nf, d->E.d_nface + i, sizeof(nf), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(&fs, d->E.d_fstart + i, sizeof(fs), cudaMemcpyDeviceToHost));
+    if (count) *count = nf;
+    if (nf > cap) return fail(TESS_E_CAPACITY, "cell %zu has %u faces, capacity %zu", i, nf, cap);
+    if (nf) {
+        if (nbr) CU(cudaMemcpy(nbr, d->E.d_fnbr + fs, sizeof(int32_t) * nf, cudaMemcpyDeviceToHost));
+        if (area) CU(cudaMemcpy(area, d->E.d_farea + fs, sizeof(double) * nf, cudaMemcpyDeviceToHost));
+    }
+    return TESS_OK;
+}
+
+tess_status tess_cell_neighbors(const tess_diagram* d, size_t i, int32_t* nbr, size_t cap, size_t* count) {
+    return tess_cell_faces(d, i, nbr, nullptr, cap, count);
+}
+
+tess_status tess_cell_original_index(const tess_diagram* d, size_t i, size_t* original) {
+    if (!d || !original) return fail(TESS_E_INVALID, "NULL argument");
+    if (i >= d->n) return fail(TESS_E_INVALID, "cell index %zu out of range", i);
+    *original = i;
+    return TESS_OK;
+}
+
+static tess_status geo_for(tess_diagram* d, size_t i, GeoOut* g) {
+    TRY(cell_check(d, i));
+    uint32_t gs = 0;
+    CU(cudaSetDevice(d->E.device));
+    CU(cudaMemcpy(&gs, d->E.d_inv + i, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return engine_geo(d->E, d->E.last_precision, gs, nullptr, d->E.last_radius, d->E.last_group, nullptr, nullptr, g);
+}
+
+tess_status tess_cell_vertices(tess_diagram* d, size_t i, double* xyz, size_t cap, size_t* count) {
+    GeoOut* g = new (std::nothrow) GeoOut;
+    if (!g) return fail(TESS_E_NOMEM, "host allocation failed");
+    tess_status st = geo_for(d, i, g);
+    if (st == TESS_OK) {
+        if (count) *count = (size_t)g->nv;
+        if ((size_t)g->nv > cap) st = fail(TESS_E_CAPACITY, "cell %zu has %d vertices, capacity %zu", i, g->nv, cap);
+        else if (xyz) memcpy(xyz, g->verts, sizeof(double) * 3 * g->nv);
+    }
+    delete g;
+    return st;
+}
+
+tess_status tess_cell_face_vertices(tess_diagram* d, size_t i, size_t face, double* xyz, size_t cap,
+                                    size_t* count) {
+    GeoOut* g = new (std::nothrow) GeoOut;
+    if (!g) return fail(TESS_E_NOMEM, "host allocation failed");
+    tess_status st = geo_for(d, i, g);
+    if (st == TESS_OK) {
+        if (face >= (size_t)g->nf) {
+            st = fail(TESS_E_INVALID, "face %zu out of range (%d faces)", face, g->nf);
+        } else {
+            const int b = g->face_off[face], e = g->face_off[face + 1];
+            if (count) *count = (size_t)(e - b);
+            if ((size_t)(e - b) > cap) st = fail(TESS_E_CAPACITY, "face has %d vertices, capacity %zu", e - b, cap);
+            else if (xyz)
+                for (int t = b; t < e; ++t) memcpy(xyz + 3 * (t - b), g->verts + 3 * g->face_vtx[t], 3 * sizeof(double));
+        }
+    }
+    delete g;
+    return st;
+}
+
+static void geo_to_public(const GeoOut& g, tess_cell_geometry* out) {
+    out->volume = g.volume;
+    out->nvertices = g.nv;
+    out->nfaces = g.nf;
+    memcpy(out->vertices, g.verts, sizeof(out->vertices));
+    memcpy(out->face_neighbor, g.face_nbr, sizeof(out->face_neighbor));
+    memcpy(out->face_area, g.face_area, sizeof(out->face_area));
+    memcpy(out->face_offset, g.face_off, sizeof(out->face_offset));
+    memcpy(out->face_vertex, g.face_vtx, sizeof(out->face_vertex));
+}
+
+static tess_status single_cell(tess_diagram* d, const size_t* i, const double* p, tess_precision precision,
+                               double search_radius, int64_t target_group, const double lo[3], const double hi[3],
+                               tess_cell_geometry* out) {
+    if (!d || !out) return fail(TESS_E_INVALID, "NULL argument");
+    if (!d->E.built) return fail(TESS_E_STATE, "diagram is not built");
+    if ((lo == nullptr) != (hi == nullptr)) return fail(TESS_E_INVALID, "give both lo and hi, or neither");
+    if (lo) TRY(validate_box(lo, hi));
+    if ((int)precision != TESS_PRECISION_FP64 && (int)precision != TESS_PRECISION_FP32_GUARD)
+        return fail(TESS_E_INVALID, "unknown precision %d", (int)precision);
+    if (std::isnan(search_radius)) return fail(TESS_E_INVALID, "search_radius is NaN");
+    uint32_t gs = 0;
+    CU(cudaSetDevice(d->E.device));
+    if (i) {
+        if (*i >= d->n) return fail(TESS_E_INVALID, "cell index %zu out of range (n = %u)", *i, d->n);
+        CU(cudaMemcpy(&gs, d->E.d_inv + *i, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    } else if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[2])) {
+        return fail(TESS_E_INVALID, "point must be finite");
+    }
+    GeoOut* g = new (std::nothrow) GeoOut;
+    if (!g) return fail(TESS_E_NOMEM, "host allocation failed");
+    tess_status st = engine_geo(d->E, (int)precision, gs, i ? nullptr : p, search_radius, target_group, lo, hi, g);
+    if (st == TESS_OK) geo_to_public(*g, out);
+    delete g;
+    return st;
+}
+
+tess_status tess_cell_compute(tess_diagram* d, size_t i, tess_precision precision, double search_radius,
+                              int64_t target_group, const double lo[3], const double hi[3],
+                              tess_cell_geometry* out) {
+    return single_cell(d, &i, nullptr, precision, search_radius, target_group, lo, hi, out);
+}
+
+tess_status tess_cell_compute_at(tess_diagram* d, const double p[3], tess_precision precision,
+                                 double search_radius, int64_t target_group, const double lo[3],
+                                 const double hi[3], tess_cell_geometry* out) {
+    if (!p) return fail(TESS_E_INVALID, "point is NULL");
+    return single_cell(d, nullptr, p, precision, search_radius, target_group, lo, hi, out);
+}
+
+tess_status tess_volumes(tess_diagram* d, double* volumes) {
+    if (!d || !volumes) return fail(TESS_E_INVALID, "NULL argument");
+    if (!d->E.computed) return fail(TESS_E_STATE, "compute_all has not run");
+    CU(cudaSetDevice(d->E.device));
+    CU(cudaMemcpyAsync(volumes, d->E.d_vol, sizeof(double) * d->n, cudaMemcpyDeviceToHost, d->E.stream));
+    CU(cudaStreamSynchronize(d->E.stream));
+    return TESS_OK;
+}
+
+static tess_status csr_out(Engine& E, uint64_t* offs, int32_t* nbr, double* area, size_t cap, size_t* total) {
+    TRY(engine_csr(E));
+    if (total) *total = E.csr_total;
+    CU(cudaSetDevice(E.device));
+    if (offs) CU(cudaMemcpyAsync(offs, E.d_offs, sizeof(uint64_t) * (E.total + 1), cudaMemcpyDeviceToHost, E.stream));
+    if ((nbr || area) && E.csr_total > cap) {
+        CU(cudaStreamSynchronize(E.stream));
+        return fail(TESS_E_CAPACITY, "%llu faces, capacity %zu", (unsigned long long)E.csr_total, cap);
+    }
+    if (nbr && E.csr_total)
+        CU(cudaMemcpyAsync(nbr, E.d_cnbr, sizeof(int32_t) * E.csr_total, cudaMemcpyDeviceToHost, E.stream));
+    if (area && E.csr_total)
+        CU(cudaMemcpyAsync(area, E.d_carea, sizeof(double) * E.csr_total, cudaMemcpyDeviceToHost, E.stream));
+    CU(cudaStreamSynchronize(E.stream));
+    return TESS_OK;
+}
+
+tess_status tess_neighbors_csr(tess_diagram* d, uint64_t* offs, int32_t* nbr, double* area, size_t cap,
+                               size_t* total) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    return csr_out(d->E, offs, nbr, area, cap, total);
+}
+
+tess_status tess_results_device(tess_diagram* d, const double** volumes, const uint64_t** offs,
+                                const int32_t** nbr, const double** area, size_t* total) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    TRY(engine_csr(d->E));
+    if (volumes) *volumes = d->E.d_vol;
+    if (offs) *offs = d->E.d_offs;
+    if (nbr) *nbr = d->E.d_cnbr;
+    if (area) *area = d->E.d_carea;
+    if (total) *total = d->E.csr_total;
+    return TESS_OK;
+}
+
+// ---- batch ----
+tess_status tess_batch_create(size_t ndiag, const uint64_t* pt_offsets, const double* xyz, const double* boxes,
+                              const tess_config* cfg, tess_batch** out) {
+    if (!out) return fail(TESS_E_INVALID, "out is NULL");
+    *out = nullptr;
+    if (ndiag == 0 || !pt_offsets || !xyz || !boxes) return fail(TESS_E_INVALID, "NULL or empty argument");
+    if (pt_offsets[0] != 0) return fail(TESS_E_INVALID, "pt_offsets[0] must be 0");
+    std::vector<DiagDesc> v(ndiag);
+    for (size_t d = 0; d < ndiag; ++d) {
+        if (pt_offsets[d + 1] <= pt_offsets[d]) return fail(TESS_E_INVALID, "diagram %zu is empty", d);
+        if (pt_offsets[d + 1] >= 0xFFFFFFF0ull) return fail(TESS_E_INVALID, "too many points");
+        DiagDesc& D = v[d];
+        memset(&D, 0, sizeof(D));
+        D.pt_base = (uint32_t)pt_offsets[d];
+        D.n = (uint32_t)(pt_offsets[d + 1] - pt_offsets[d]);
+        TRY(validate_box(boxes + 6 * d, boxes + 6 * d + 3));
+        for (int a = 0; a < 3; ++a) {
+            D.blo[a] = boxes[6 * d + a];
+            D.bhi[a] = boxes[6 * d + 3 + a];
+        }
+    }
+    tess_batch* h = new (std::nothrow) tess_batch();
+    if (!h) return fail(TESS_E_NOMEM, "host allocation failed");
+    tess_status st = engine_init(h->E, cfg, v, xyz, false, nullptr);
+    if (st == TESS_OK) st = engine_build(h->E, true);
+    if (st != TESS_OK) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    return TESS_OK;
+}
+
+tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
+    if (!b) return fail(TESS_E_INVALID, "batch is NULL");
+    Engine& E = b->E;
+    const int prec = (int)precision;
+    if (prec != TESS_PRECISION_FP64 && prec != TESS_PRECISION_FP32_GUARD)
+        return fail(TESS_E_INVALID, "unknown precision %d", prec);
+    CU(cudaSetDevice(E.device));
+    if (!E.graph || E.graph_precision != prec) {
+        // warm the per-kernel attributes and occupancy queries outside capture
+        for (int pr : {0, 1})
+            for (int s : {2, 4, 8}) E.blocks(pr, s);
+        if (E.graph) cudaGraphExecDestroy(E.graph);
+        E.graph = nullptr;
+        cudaGraph_t g = nullptr;
+        CU(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
+        tess_status st = TESS_OK;
+        cudaError_t ce = launch_grid_build(grid_buffers(E), E.stream);
+        if (ce != cudaSuccess) st = fail(TESS_E_CUDA, "capture: %s", cudaGetErrorString(ce));
+        if (st == TESS_OK) st = enqueue_passes(E, prec, -1.0, -1, false, nullptr);
+        cudaError_t ee = cudaStreamEndCapture(E.stream, &g);
+        if (st != TESS_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (ee != cudaSuccess) return fail(TESS_E_CUDA, "end capture: %s", cudaGetErrorString(ee));
+        ce = cudaGraphInstantiate(&E.graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return fail(TESS_E_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+        E.graph_precision = prec;
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
+    if (timing) {
+        CU(cudaEventCreate(&e0));
+        CU(cudaEventCreate(&e1));
+        CU(cudaEventRecord(e0, E.stream));
+    }
+    CU(cudaGraphLaunch(E.graph, E.stream));
+    E.launches += kGridLaunches + (prec == 1 ? 6 : 3);
+    if (timing) CU(cudaEventRecord(e1, E.stream));
+    unsigned long long used = 0;
+    unsigned counts[16];
+    CU(cudaMemcpyAsync(&used, E.d_fcursor, sizeof(used), cudaMemcpyDeviceToHost, E.stream));
+    CU(cudaMemcpyAsync(counts, E.d_counters + 16, sizeof(counts), cudaMemcpyDeviceToHost, E.stream));
+    CU(cudaStreamSynchronize(E.stream));
+    if (timing) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        E.stats.ms_clip = ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    if (used > E.face_cap) {
+        // grow the pool; the captured graph holds the old pointer
+        dfree(E.d_fnbr);
+        dfree(E.d_farea);
+        E.face_cap = used + used / 4 + 4096;
+        TRY(dalloc(&E.d_fnbr, E.face_cap));
+        TRY(dalloc(&E.d_farea, E.face_cap));
+        cudaGraphExecDestroy(E.graph);
+        E.graph = nullptr;
+        return tess_batch_compute(b, precision);
+    }
+    E.stats.cells = E.total;
+    E.stats.faces = used;
+    E.stats.rerun_fp64 = prec == 1 ? counts[L_FP64] : 0;
+    E.stats.rerun_capacity = (uint64_t)counts[L_CAP1] + counts[L_CAP2] + counts[L_CAP64A] + counts[L_CAP64B];
+    E.stats.failed = counts[L_FAIL];
+    E.computed = true;
+    E.csr_valid = false;
+    E.last_precision = prec;
+    if (counts[L_FAIL]) return fail(TESS_E_OVERFLOW, "%u cells could not be computed", counts[L_FAIL]);
+    return TESS_OK;
+}
+
+tess_status tess_batch_stats(const tess_batch* b, tess_stats* out) {
+    if (!b || !out) return fail(TESS_E_INVALID, "NULL argument");
+    *out = b->E.stats;
+    out->launches = b->E.launches;
+    return TESS_OK;
+}
+
+tess_status tess_batch_volumes(tess_batch* b, double* volumes) {
+    if (!b || !volumes) return fail(TESS_E_INVALID, "NULL argument");
+    if (!b->E.computed) return fail(TESS_E_STATE, "compute has not run");
+    CU(cudaSetDevice(b->E.device));
+    CU(cudaMemcpyAsync(volumes, b->E.d_vol, sizeof(double) * b->E.total, cudaMemcpyDeviceToHost, b->E.stream));
+    CU(cudaStreamSynchronize(b->E.stream));
+    return TESS_OK;
+}
+
+tess_status tess_batch_neighbors_csr(tess_batch* b, uint64_t* offs, int32_t* nbr, double* area, size_t cap,
+                                     size_t* total) {
+    if (!b) return fail(TESS_E_INVALID, "batch is NULL");
+    return csr_out(b->E, offs, nbr, area, cap, total);
+}
+
+tess_status tess_batch_destroy(tess_batch* b) {
+    delete b;
+    return TESS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+// tess_clip.cu -- dispatch to the clipping kernel instantiations
+// (tess_clip_f32.cu, tess_clip_f64.cu; kernel source tess_clip_impl.cuh) and
+// the CSR compaction of the per-cell face lists: offsets = exclusive scan of
+// the face counts, then a gather from the face pool into original cell order
+// (the bulk form of Cell::compute_faces, interface.rs:373-384).
+#include "tess_internal.cuh"
+
+namespace tess {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// ---- CSR compaction: offsets = exclusive scan of face counts, then gather ----
+constexpr int kCsrThreads = 1024;
+constexpr int kCsrItems = 4;
+
+__device__ unsigned long long block_excl_scan64(unsigned long long v, unsigned long long* sh) {
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    unsigned long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long t = __shfl_up_sync(FULL, inc, o);
+        if (l >= o) inc += t;
+    }
+    if (l == 31) sh[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        unsigned long long s = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0ull;
+        unsigned long long si = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long t = __shfl_up_sync(FULL, si, o);
+            if (l >= o) si += t;
+        }
+        sh[l] = si - s;
+        if (l == 31) sh[32] = si;
+    }
+    __syncthreads();
+    const unsigned long long r = inc - v + sh[w];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kCsrThreads) k_csr_partial(const uint32_t* cnt, uint32_t n,
+                                                             unsigned long long* sums) {
+    __shared__ unsigned long long sh[33];
+    const uint64_t base = ((uint64_t)blockIdx.x * kCsrThreads + threadIdx.x) * kCsrItems;
+    unsigned long long s = 0;
+    for (int k = 0; k < kCsrItems; ++k) s += (base + k < n) ? cnt[base + k] : 0u;
+    unsigned long long ex = block_excl_scan64(s, sh);
+    if (threadIdx.x == kCsrThreads - 1) sums[blockIdx.x] = ex + s;
+}
+
+__global__ void __launch_bounds__(kCsrThreads) k_csr_sums(unsigned long long* sums, uint32_t nb) {
+    __shared__ unsigned long long sh[33];
+    unsigned long long carry = 0;
+    for (uint32_t b0 = 0; b0 < nb; b0 += kCsrThreads) {
+        const uint32_t b = b0 + threadIdx.x;
+        const unsigned long long v = b < nb ? sums[b] : 0ull;
+        const unsigned long long ex = block_excl_scan64(v, sh);
+        if (b < nb) sums[b] = carry + ex;
+        __shared__ unsigned long long tot;
+        if (threadIdx.x == kCsrThreads - 1) tot = ex + v;
+        __syncthreads();
+        carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) sums[nb] = carry;
+}
+
+__global__ void __launch_bounds__(kCsrThreads) k_csr_final(const uint32_t* cnt, uint32_t n,
+                                                           const unsigned long long* sums, uint64_t* offs) {
+    __shared__ unsigned long long sh[33];
+    const uint64_t base = ((uint64_t)blockIdx.x * kCsrThreads + threadIdx.x) * kCsrItems;
+    uint32_t v[kCsrItems];
+    unsigned long long s = 0;
+    for (int k = 0; k < kCsrItems; ++k) {
+        v[k] = (base + k < n) ? cnt[base + k] : 0u;
+        s += v[k];
+    }
+    unsigned long long run = sums[blockIdx.x] + block_excl_scan64(s, sh);
+    for (int k = 0; k < kCsrItems; ++k) {
+        if (base + k < n) offs[base + k] = run;
+        run += v[k];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) offs[n] = sums[gridDim.x];
+}
+
+__global__ void k_csr_gather(const uint32_t* cnt, const uint64_t* fstart, const int32_t* fnbr,
+                             const double* farea, uint32_t n, const uint64_t* offs, int32_t* nbr,
+                             double* area) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t src = fstart[i], dst = offs[i];
+    const uint32_t c = cnt[i];
+    for (uint32_t t = 0; t < c; ++t) {
+        if (nbr) nbr[dst + t] = fnbr[src + t];
+        if (area) area[dst + t] = farea[src + t];
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_clip(const ClipParams& p, int precision, int slots, int wpb, int blocks, cudaStream_t s) {
+    return precision == 1 ? launch_clip_f32(p, slots, wpb, blocks, s) : launch_clip_f64(p, slots, wpb, blocks, s);
+}
+
+int clip_blocks_for(int precision, int slots, int wpb, int device) {
+    return precision == 1 ? clip_blocks_f32(slots, wpb, device) : clip_blocks_f64(slots, wpb, device);
+}
+
+size_t csr_tmp_words(uint32_t n) {
+    const uint64_t per = (uint64_t)kCsrThreads * kCsrItems;
+    return (size_t)((n + per - 1) / per) + 2;
+}
+
+cudaError_t launch_csr_offsets(const uint32_t* nface, uint32_t n, uint64_t* offs, uint64_t* scan_tmp,
+                               cudaStream_t s) {
+    const uint64_t per = (uint64_t)kCsrThreads * kCsrItems;
+    const uint32_t nb = (uint32_t)((n + per - 1) / per);
+    unsigned long long* sums = reinterpret_cast<unsigned long long*>(scan_tmp);
+    k_csr_partial<<<nb, kCsrThreads, 0, s>>>(nface, n, sums);
+    k_csr_sums<<<1, kCsrThreads, 0, s>>>(sums, nb);
+    k_csr_final<<<nb, kCsrThreads, 0, s>>>(nface, n, sums, offs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_csr_gather(const uint32_t* nface, const uint64_t* fstart, const int32_t* face_nbr,
+                              const double* face_area, uint32_t n, const uint64_t* offs, int32_t* nbr_out,
+                              double* area_out, cudaStream_t s) {
+    k_csr_gather<<<(n + 255) / 256, 256, 0, s>>>(nface, fstart, face_nbr, face_area, n, offs, nbr_out, area_out);
+    return cudaGetLastError();
+}
+
+}  // namespace tess

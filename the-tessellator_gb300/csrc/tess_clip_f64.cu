@@ -1,0 +1,22 @@
+// tess_clip_f64.cu -- FP64 instantiations of the clipping kernel (the
+// plain FP64 form and the FP64 re-runs); kernel source in tess_clip_impl.cuh.
+#include "tess_clip_impl.cuh"
+
+namespace tess {
+
+cudaError_t launch_clip_f64(const ClipParams& p, int slots, int wpb, int blocks, cudaStream_t s) {
+    using namespace clipk;
+    const bool geo = p.geo != nullptr;
+    if (slots <= 2) return geo ? launch_t<double, 2, true>(p, wpb, blocks, s) : launch_t<double, 2, false>(p, wpb, blocks, s);
+    if (slots <= 4) return geo ? launch_t<double, 4, true>(p, wpb, blocks, s) : launch_t<double, 4, false>(p, wpb, blocks, s);
+    return geo ? launch_t<double, 8, true>(p, wpb, blocks, s) : launch_t<double, 8, false>(p, wpb, blocks, s);
+}
+
+int clip_blocks_f64(int slots, int wpb, int device) {
+    using namespace clipk;
+    if (slots <= 2) return blocks_t<double, 2, false>(wpb, device);
+    if (slots <= 4) return blocks_t<double, 4, false>(wpb, device);
+    return blocks_t<double, 8, false>(wpb, device);
+}
+
+}  // namespace tess

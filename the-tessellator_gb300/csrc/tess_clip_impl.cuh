@@ -1,0 +1,827 @@
+// tess_clip.cu -- the clipping kernel: one Voronoi cell per warp.
+//
+// The GPU form of Cell::compute_voronoi_cell (interface.rs:257-313) with
+// Polyhedron::cut_with_plane (polyhedron.rs:438-642), ExpandingSearch
+// (celery.rs:865-1075) and the cell outputs (polyhedron.rs:776-935).
+//
+// Cell representation (per warp).  The polyhedron starts as the container
+// box translated by -site (polyhedron.rs:268-392, interface.rs:266).  Every
+// vertex is the meeting point of three face planes and is stored as
+//   - its position: in lane registers (slot s lives in lane s % 32, register
+//     set s / 32) with a mirror in shared memory,
+//   - its plane triple (a, b, c), ordered counter-clockwise seen from outside,
+//   - its three neighbours: adj[i] is the vertex across the edge (t[i], t[i+1]).
+// The half-edge pools of the reference (pool.rs) become these fixed-capacity
+// slot arrays; a cell that outgrows them is flagged and re-run at a larger
+// capacity.
+//
+// Cutting by a bisector (vector3.rs:223-239):
+//   1. every lane classifies its vertices, sd = n.v - offset, Outside when
+//      sd > 1e-12 (vector3.rs:170-193, polyhedron.rs:221); one ballot per
+//      register set gives the Outside mask.  No Outside vertex: no cut.
+//   2. an edge of an Outside vertex X whose neighbour Y is not Outside is a
+//      boundary edge; it gets a new vertex at the reference's intersection
+//      X + (Y - X) * sd_X / (sd_X - sd_Y) (vector3.rs:213-219) with the
+//      triple (a, b, new plane).  An Incident Y (|sd| <= tol) yields a
+//      vertex at Y's position, as the reference duplicates Incident vertices
+//      (polyhedron.rs:554-565).
+//   3. the new vertices link into a ring through two small maps
+//      (first plane -> vertex, second plane -> vertex), Outside slots are
+//      freed and reused (clean_up_vertices / clean_up_edges, polyhedron.rs:645-730).
+//
+// Candidates come bin by bin in shell order (get_search_order,
+// celery.rs:418-679) and the walk stops once the next bin's gap distance is
+// at least twice the largest vertex distance: no farther point can cut
+// (the security radius; the reference walks every point instead,
+// celery.rs:971-1018, with the same result).
+//
+// FP32 form: positions, planes and classification in FP32; any live vertex
+// with |sd| below guard_rel * R (R = cell radius) aborts the cell, which is
+// then re-run in FP64.  Areas and volumes are accumulated in FP64 in both
+// forms (weighted normals and volume / 6, polyhedron.rs:776-855).
+#include <cfloat>
+#include <cmath>
+
+#pragma once
+#include "tess_internal.cuh"
+
+namespace tess {
+namespace clipk {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <typename T, int K>
+struct Smem {
+    static constexpr int V = 32 * K;                                 // vertex slots
+    static constexpr int P = (32 * K + 32) < 254 ? (32 * K + 32) : 254;  // planes (< 0xFF)
+    static constexpr int VUSE = V < 255 ? V : 255;                    // slot 255 is the map sentinel
+    T px[P], py[P], pz[P], pd[P];     // plane: unit normal, offset
+    T vx[V], vy[V], vz[V], vsd[V];    // vertex mirror, signed distances
+    int32_t pid[P];                   // neighbour id (local original index) or wall code
+    uint32_t tri[V];                  // planes a | b << 8 | c << 16
+    uint32_t adj[V];                  // neighbours n0 | n1 << 8 | n2 << 16
+    uint32_t fdeg[P];                 // finalize: live vertices per face
+    uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
+    int32_t flist[P];                 // finalize: compacted face ids
+    uint8_t fsta[P];                  // finalize: one vertex of each face
+    uint8_t mapf[P], maps[P];         // new-vertex ring maps
+    uint8_t rank2p[P];                // geometry output: rank -> plane
+};
+
+__device__ __forceinline__ unsigned warp_incl_scan_u(unsigned v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned t = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_max_t(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+
+// Position of the q-th (0-based) set bit of m; requires q < popc(m).
+__device__ __forceinline__ int select32(uint32_t m, int q) {
+    int pos = 0;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        const uint32_t low = (1u << (pos + s)) - 1u;
+        if (__popc(m & low) <= q) pos += s;
+    }
+    return pos;
+}
+
+template <int K>
+__device__ __forceinline__ int select_k(const uint32_t (&m)[K], int q) {
+    int res = -1;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int c = __popc(m[k]);
+        if (res < 0) {
+            if (q < c) res = k * 32 + select32(m[k], q);
+            else q -= c;
+        }
+    }
+    return res;
+}
+
+template <int K>
+__device__ __forceinline__ bool bit_k(const uint32_t (&m)[K], int s) {
+    uint32_t w = m[0];
+#pragma unroll
+    for (int k = 1; k < K; ++k)
+        if ((s >> 5) == k) w = m[k];
+    return (w >> (s & 31)) & 1u;
+}
+
+template <int K>
+__device__ __forceinline__ void set_k(uint32_t (&m)[K], int s) {
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if ((s >> 5) == k) m[k] |= 1u << (s & 31);
+}
+
+__device__ __forceinline__ int plane_of(uint32_t t, int i) { return (int)((t >> (8 * i)) & 0xFFu); }
+
+// Signed distance n.v - offset.
+__device__ __forceinline__ float sdist(float nx, float ny, float nz, float off, float x, float y, float z) {
+    return fmaf(nx, x, fmaf(ny, y, fmaf(nz, z, -off)));
+}
+__device__ __forceinline__ double sdist(double nx, double ny, double nz, double off, double x, double y,
+                                        double z) {
+    return fma(nx, x, fma(ny, y, fma(nz, z, -off)));
+}
+
+// Bisector of the site (origin) and r (halfway_from_origin_to, vector3.rs:223-239).
+__device__ __forceinline__ void bisector(float rx, float ry, float rz, float r2, float& nx, float& ny,
+                                         float& nz, float& off) {
+    const float inv = rsqrtf(r2);
+    nx = rx * inv;
+    ny = ry * inv;
+    nz = rz * inv;
+    off = 0.5f * r2 * inv;
+}
+__device__ __forceinline__ void bisector(double rx, double ry, double rz, double r2, double& nx,
+                                         double& ny, double& nz, double& off) {
+    const double inv = 1.0 / sqrt(r2);
+    nx = rx * inv;
+    ny = ry * inv;
+    nz = rz * inv;
+    off = nx * (rx * 0.5) + ny * (ry * 0.5) + nz * (rz * 0.5);
+}
+
+template <typename T, int K>
+struct CellRegs {
+    T vx[K], vy[K], vz[K];
+    uint32_t lm[K];   // live masks (warp-uniform)
+    int np;           // planes used (warp-uniform)
+};
+
+// Clip the cell by {x : n.x - off <= 0}.  Returns 1 when vertices were cut
+// off, 0 when nothing was Outside, or -status.
+template <typename T, int K, bool GUARD>
+__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, int32_t id, T guard,
+                   int lane) {
+    using S_t = Smem<T, K>;
+    T sd[K];
+    uint32_t om[K];
+    bool gh = false;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const bool live = (C.lm[k] >> lane) & 1u;
+        sd[k] = sdist(nx, ny, nz, off, C.vx[k], C.vy[k], C.vz[k]);
+        const bool out = live && sd[k] > (T)kTolerance;
+        if (GUARD) gh |= live && fabs(sd[k]) < guard;
+        om[k] = __ballot_sync(FULL, out);
+    }
+    if (GUARD && __any_sync(FULL, gh)) return -ST_GUARD;
+    uint32_t anyo = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) anyo |= om[k];
+    if (!anyo) return 0;
+    if (C.np >= S_t::P) return -ST_PCAP;
+
+    // Signed distances of live vertices, read by the lanes owning Outside
+    // neighbours; triples/neighbours of my Outside vertices, read before any
+    // slot is reused.
+    uint32_t xt[K], xa[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int s = k * 32 + lane;
+        if ((C.lm[k] >> lane) & 1u) S.vsd[s] = sd[k];
+        xt[k] = 0;
+        xa[k] = 0;
+        if ((om[k] >> lane) & 1u) {
+            xt[k] = S.tri[s];
+            xa[k] = S.adj[s];
+        }
+    }
+    // Every slot and plane id read below must be in range; a violation
+    // (inconsistent topology) abandons the cell before anything is written.
+    bool badref = false;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if ((om[k] >> lane) & 1u) {
+#pragma unroll
+            for (int e = 0; e < 3; ++e)
+                badref |= plane_of(xt[k], e) >= C.np || plane_of(xa[k], e) >= S_t::V;
+        }
+    }
+    if (__any_sync(FULL, badref)) return -ST_DEGEN;
+    unsigned bnd = 0;
+    int cnt = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if ((om[k] >> lane) & 1u) {
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                const int nb = plane_of(xa[k], e);
+                if (!bit_k<K>(om, nb)) {
+                    bnd |= 1u << (3 * k + e);
+                    ++cnt;
+                }
+            }
+        }
+    }
+    const unsigned incl = warp_incl_scan_u((unsigned)cnt, lane);
+    const int B = (int)__shfl_sync(FULL, incl, 31);
+    int q = (int)incl - cnt;
+    int nlive = 0;
+    uint32_t fm[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const uint32_t keep = C.lm[k] & ~om[k];
+        nlive += __popc(keep);
+        fm[k] = ~keep;
+    }
+    if (K == 8) fm[K - 1] &= 0x7FFFFFFFu;
+    if (nlive + B > S_t::VUSE) return -ST_VCAP;
+    __syncwarp();
+
+    // Pass 1: place the new vertices.
+    uint32_t newm[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) newm[k] = 0;
+    int nslot[3 * K], na[3 * K], nbp[3 * K], ny_[3 * K];
+    const int f = C.np;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            const int c = 3 * k + e;
+            nslot[c] = -1;
+            if (bnd & (1u << c)) {
+                const int a = plane_of(xt[k], e);
+                const int b = plane_of(xt[k], (e + 1) % 3);
+                const int y = plane_of(xa[k], e);
+                const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
+                const T xsd = sd[k];
+                const T t = xsd / (xsd - ysd);
+                const T px = C.vx[k] + (yx - C.vx[k]) * t;
+                const T py = C.vy[k] + (yy - C.vy[k]) * t;
+                const T pz = C.vz[k] + (yz - C.vz[k]) * t;
+                const int slot = select_k<K>(fm, q);
+                ++q;
+                S.vx[slot] = px;
+                S.vy[slot] = py;
+                S.vz[slot] = pz;
+                S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
+                // Y's pointer back to X is the edge (b, a) of Y's triple.
+                const uint32_t ty = S.tri[y];
+                const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
+                               : (plane_of(ty, 1) == b && plane_of(ty, 2) == a) ? 1
+                                                                                : 2;
+                reinterpret_cast<uint8_t*>(S.adj)[4 * y + yi] = (uint8_t)slot;
+                S.mapf[a] = (uint8_t)slot;
+                S.maps[b] = (uint8_t)slot;
+                set_k<K>(newm, slot);
+                nslot[c] = slot;
+                na[c] = a;
+                nbp[c] = b;
+                ny_[c] = y;
+            }
+        }
+    }
+    __syncwarp();
+    // Pass 2: link the ring of new vertices.
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < 3 * K; ++c) {
+        if (nslot[c] >= 0) {
+            const int n1 = S.mapf[nbp[c]];
+            const int n2 = S.maps[na[c]];
+            bad |= (S.mapf[na[c]] != nslot[c]) || (S.maps[nbp[c]] != nslot[c]) || n1 == 0xFF || n2 == 0xFF;
+            S.adj[nslot[c]] = (uint32_t)ny_[c] | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int c = 0; c < 3 * K; ++c) {
+        if (nslot[c] >= 0) {
+            S.mapf[na[c]] = 0xFF;
+            S.maps[nbp[c]] = 0xFF;
+        }
+    }
+    if (__any_sync(FULL, bad)) return -ST_DEGEN;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        newm[k] = __reduce_or_sync(FULL, newm[k]);
+        C.lm[k] = (C.lm[k] & ~om[k]) | newm[k];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if ((newm[k] >> lane) & 1u) {
+            const int s = k * 32 + lane;
+            C.vx[k] = S.vx[s];
+            C.vy[k] = S.vy[s];
+            C.vz[k] = S.vz[s];
+        }
+    }
+    if (lane == 0) {
+        S.px[f] = nx;
+        S.py[f] = ny;
+        S.pz[f] = nz;
+        S.pd[f] = off;
+        S.pid[f] = id;
+    }
+    C.np = f + 1;
+    __syncwarp();
+    return 1;
+}
+
+template <typename T, int K>
+__device__ __forceinline__ T live_r2(const CellRegs<T, K>& C, int lane) {
+    T r2 = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if ((C.lm[k] >> lane) & 1u) r2 = max(r2, C.vx[k] * C.vx[k] + C.vy[k] * C.vy[k] + C.vz[k] * C.vz[k]);
+    return warp_max_t(r2);
+}
+
+__device__ __forceinline__ void ring_offset(int s, uint32_t r, int& i, int& j, int& k) {
+    const uint32_t a = 2u * s + 1u, b = 2u * s - 1u;
+    const uint32_t nx = 2u * a * a, ny = 2u * b * a;
+    if (r < nx) {
+        const uint32_t side = r / (a * a), rem = r % (a * a);
+        i = side ? s : -s;
+        j = (int)(rem / a) - s;
+        k = (int)(rem % a) - s;
+    } else if (r < nx + ny) {
+        r -= nx;
+        const uint32_t side = r / (b * a), rem = r % (b * a);
+        j = side ? s : -s;
+        i = (int)(rem / a) - (s - 1);
+        k = (int)(rem % a) - s;
+    } else {
+        r -= nx + ny;
+        const uint32_t side = r / (b * b), rem = r % (b * b);
+        k = side ? s : -s;
+        i = (int)(rem / b) - (s - 1);
+        j = (int)(rem % b) - (s - 1);
+    }
+}
+
+template <typename T, int K, bool GEO>
+__device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int lane) {
+    using S_t = Smem<T, K>;
+    constexpr bool GUARD = sizeof(T) == 4;
+    // ---- diagram of this cell ----
+    int d = 0;
+    if (P.ndiag > 1 && !P.at_point) {
+        int lo = 0, hi = P.ndiag - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (P.diags[mid].pt_base <= gs) lo = mid;
+            else hi = mid - 1;
+        }
+        d = lo;
+    }
+    const DiagDesc& D = P.diags[d];
+    double sx, sy, sz;
+    uint32_t self = 0xFFFFFFFFu, orig = 0;
+    if (P.at_point) {
+        sx = P.point[0];
+        sy = P.point[1];
+        sz = P.point[2];
+    } else {
+        sx = P.spx[gs];
+        sy = P.spy[gs];
+        sz = P.spz[gs];
+        self = gs;
+        orig = P.sorted[gs];
+    }
+
+    // ---- the container box, translated by -site (polyhedron.rs:268-392) ----
+    const double* blo = P.box_override ? P.box : D.blo;
+    const double* bhi = P.box_override ? P.box + 3 : D.bhi;
+    CellRegs<T, K> C;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        C.vx[k] = C.vy[k] = C.vz[k] = (T)0;
+        C.lm[k] = 0;
+    }
+    C.lm[0] = 0xFFu;
+    C.np = 6;
+    if (lane < 6) {
+        const int a = lane >> 1;
+        const bool mx = lane & 1;
+        const double s_a = a == 0 ? sx : (a == 1 ? sy : sz);
+        const double off = mx ? (bhi[a] - s_a) : (s_a - blo[a]);
+        const T sg = mx ? (T)1 : (T)-1;
+        S.px[lane] = a == 0 ? sg : (T)0;
+        S.py[lane] = a == 1 ? sg : (T)0;
+        S.pz[lane] = a == 2 ? sg : (T)0;
+        S.pd[lane] = (T)off;
+        S.pid[lane] = -1 - lane;   // -1 x_min, -2 x_max, -3 y_min, -4 y_max, -5 z_min, -6 z_max
+    }
+    if (lane < 8) {
+        const int bx = lane & 1, by = (lane >> 1) & 1, bz = (lane >> 2) & 1;
+        C.vx[0] = (T)((bx ? bhi[0] : blo[0]) - sx);
+        C.vy[0] = (T)((by ? bhi[1] : blo[1]) - sy);
+        C.vz[0] = (T)((bz ? bhi[2] : blo[2]) - sz);
+        S.vx[lane] = C.vx[0];
+        S.vy[lane] = C.vy[0];
+        S.vz[lane] = C.vz[0];
+        const int pX = bx, pY = 2 + by, pZ = 4 + bz;
+        const int sgn = (bx ? 1 : -1) * (by ? 1 : -1) * (bz ? 1 : -1);
+        const int t0 = pX, t1 = sgn > 0 ? pY : pZ, t2 = sgn > 0 ? pZ : pY;
+        S.tri[lane] = (uint32_t)t0 | ((uint32_t)t1 << 8) | ((uint32_t)t2 << 16);
+        auto flip = [](int p) { return p < 2 ? 1 : (p < 4 ? 2 : 4); };
+        const int n0 = lane ^ flip(t2), n1 = lane ^ flip(t0), n2 = lane ^ flip(t1);
+        S.adj[lane] = (uint32_t)n0 | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
+    }
+    for (int i = lane; i < S_t::P; i += 32) {
+        S.mapf[i] = 0xFF;
+        S.maps[i] = 0xFF;
+    }
+    __syncwarp();
+    T R2 = live_r2(C, lane);
+    T guard = (T)P.guard_rel * sqrt(R2);
+    int status = ST_OK;
+
+    // ---- the walk over bins in shell order (celery.rs:1023-1075) ----
+    const int cpd = D.cpd;
+    const int cbx = axis_index(sx, D.glo[0], D.ghi[0], D.inv[0], cpd);
+    const int cby = axis_index(sy, D.glo[1], D.ghi[1], D.inv[1], cpd);
+    const int cbz = axis_index(sz, D.glo[2], D.ghi[2], D.inv[2], cpd);
+    const double radius = P.search_radius;
+    const int64_t tgroup = P.target_group;
+    const TabEntry* tab = P.table + D.tab_base;
+
+    // Cut by every point of the lane's bin (lb = global bin, or -1).
+    auto process = [&](long long lb) -> int {
+        unsigned cnt = 0, beg = 0;
+        if (lb >= 0) {
+            beg = P.delims[lb];
+            cnt = P.delims[lb + 1] - beg;
+        }
+        const unsigned incl = warp_incl_scan_u(cnt, lane);
+        const unsigned total = __shfl_sync(FULL, incl, 31);
+        S.cpref[lane] = incl - cnt;
+        S.cbeg[lane] = beg;
+        __syncwarp();
+        for (unsigned w0 = 0; w0 < total; w0 += 32) {
+            const unsigned c = w0 + lane;
+            bool keep = false;
+            T rx = 0, ry = 0, rz = 0, r2 = 0;
+            uint32_t j = 0;
+            const T lim = (T)4 * R2 * (T)kStopMargin;
+            if (c < total) {
+                int lo = 0, hi = 31;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (S.cpref[mid] <= c) lo = mid;
+                    else hi = mid - 1;
+                }
+                j = S.cbeg[lo] + (c - S.cpref[lo]);
+                rx = (T)(P.spx[j] - sx);
+                ry = (T)(P.spy[j] - sy);
+                rz = (T)(P.spz[j] - sz);
+                r2 = rx * rx + ry * ry + rz * rz;
+                keep = (j != self) && r2 > (T)0 && r2 < lim;
+                if (keep && tgroup >= 0) keep = (int64_t)(P.sgroup ? P.sgroup[j] : 0u) == tgroup;
+            }
+            unsigned km = __ballot_sync(FULL, keep);
+            while (km) {
+                const int src = __ffs(km) - 1;
+                km &= km - 1;
+                const T cx = __shfl_sync(FULL, rx, src);
+                const T cy = __shfl_sync(FULL, ry, src);
+                const T cz = __shfl_sync(FULL, rz, src);
+                const T c2 = __shfl_sync(FULL, r2, src);
+                const uint32_t cj = __shfl_sync(FULL, j, src);
+                if (!(c2 < (T)4 * R2 * (T)kStopMargin)) continue;
+                T nx, ny, nz, off;
+                bisector(cx, cy, cz, c2, nx, ny, nz, off);
+                const int32_t id = (int32_t)(P.sorted[cj] - D.pt_base);
+                const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, id, guard, lane);
+                if (r < 0) return -r;
+                if (r > 0) {
+                    R2 = live_r2(C, lane);
+                    guard = (T)P.guard_rel * sqrt(R2);
+                }
+            }
+        }
+        __syncwarp();
+        return ST_OK;
+    };
+
+    auto bin_of = [&](int i, int j, int k) -> long long {
+        const int x = cbx + i, y = cby + j, z = cbz + k;
+        if (x < 0 || x >= cpd || y < 0 || y >= cpd || z < 0 || z >= cpd) return -1;
+        return (long long)(D.bin_base + ((uint64_t)x * cpd + y) * cpd + z);
+    };
+
+    // phase 1: the sorted shell table
+    bool phase2 = false;
+    uint32_t t = 0;
+    for (;;) {
+        const double thr = 4.0 * (double)R2 * kStopMargin;
+        const uint32_t idx = t + lane;
+        bool stop = true;
+        int oi = 0, oj = 0, ok = 0;
+        if (idx < D.tab_len) {
+            const TabEntry e = tab[idx];
+            oi = e.i;
+            oj = e.j;
+            ok = e.k;
+            const double key = gap_key(D.size, oi, oj, ok);
+            stop = !(key < thr) || (radius >= 0.0 && key > radius);
+        }
+        const unsigned sm = __ballot_sync(FULL, stop);
+        const int nval = sm ? __ffs(sm) - 1 : 32;
+        long long lb = -1;
+        if (lane < nval) lb = bin_of(oi, oj, ok);
+        t += nval;
+        status = process(lb);
+        if (status != ST_OK) break;
+        if (sm) {
+            phase2 = (t >= D.tab_len) && isfinite(D.tab_kmax);
+            break;
+        }
+    }
+    // phase 2: Chebyshev rings beyond the table (sparse regions)
+    if (status == ST_OK && phase2) {
+        for (int s = 1; s <= cpd - 1 && status == ST_OK; ++s) {
+            double lbk = (double)(s - 1) * D.min_size;
+            lbk = lbk * lbk;
+            if (lbk < D.tab_kmax) lbk = D.tab_kmax;
+            if (lbk >= 4.0 * (double)R2 * kStopMargin) break;
+            if (radius >= 0.0 && lbk > radius) break;
+            const uint32_t rs = 24u * (uint32_t)s * (uint32_t)s + 2u;
+            for (uint32_t r0 = 0; r0 < rs; r0 += 32) {
+                const double thr = 4.0 * (double)R2 * kStopMargin;
+                long long lb = -1;
+                const uint32_t r = r0 + lane;
+                if (r < rs) {
+                    int i, j, k;
+                    ring_offset(s, r, i, j, k);
+                    const double key = gap_key(D.size, i, j, k);
+                    if (key > D.tab_kmax && key < thr && !(radius >= 0.0 && key > radius)) lb = bin_of(i, j, k);
+                }
+                if (!__any_sync(FULL, lb >= 0)) continue;
+                status = process(lb);
+                if (status != ST_OK) break;
+            }
+        }
+    }
+
+    // ---- finalize: faces, areas, volume in FP64 (polyhedron.rs:776-855) ----
+    int nlive = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) nlive += __popc(C.lm[k]);
+    double vol = 0.0;
+    int F = 0;
+    constexpr int R = (S_t::P + 31) / 32;
+    double farea[R];
+    int fdegr[R];
+    if (status == ST_OK) {
+        for (int i = lane; i < C.np; i += 32) S.fdeg[i] = 0;
+        __syncwarp();
+        bool fbad = false;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if ((C.lm[k] >> lane) & 1u) {
+                const int s = k * 32 + lane;
+                const uint32_t tt = S.tri[s];
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    const int p = plane_of(tt, e);
+                    if (p < C.np) {
+                        atomicAdd(&S.fdeg[p], 1u);
+                        S.fsta[p] = (uint8_t)s;
+                    } else {
+                        fbad = true;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        bool bad = fbad;
+        double vpart = 0.0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int p = r * 32 + lane;
+            farea[r] = 0.0;
+            fdegr[r] = 0;
+            if (p < C.np && S.fdeg[p] > 0) {
+                const int start = S.fsta[p];
+                int cur = start, steps = 0;
+                double ax = 0.0, ay = 0.0, az = 0.0;
+                do {
+                    const uint32_t tt = S.tri[cur], aa = S.adj[cur];
+                    const int i = plane_of(tt, 0) == p ? 0 : (plane_of(tt, 1) == p ? 1 : 2);
+                    const int nx = plane_of(aa, i);
+                    if (plane_of(tt, i) != p || nx >= S_t::V) {
+                        bad = true;
+                        break;
+                    }
+                    const double X0 = (double)S.vx[cur], X1 = (double)S.vy[cur], X2 = (double)S.vz[cur];
+                    const double Y0 = (double)S.vx[nx], Y1 = (double)S.vy[nx], Y2 = (double)S.vz[nx];
+                    // the walk runs clockwise seen from outside: Y x X is outward
+                    ax += Y1 * X2 - Y2 * X1;
+                    ay += Y2 * X0 - Y0 * X2;
+                    az += Y0 * X1 - Y1 * X0;
+                    cur = nx;
+                    ++steps;
+                } while (cur != start && steps <= S_t::V);
+                bad |= (cur != start) || (steps != (int)S.fdeg[p]) || steps < 3;
+                const double A0 = (double)S.vx[start], A1 = (double)S.vy[start], A2 = (double)S.vz[start];
+                vpart += ax * A0 + ay * A1 + az * A2;
+                farea[r] = 0.5 * sqrt(ax * ax + ay * ay + az * az);
+                fdegr[r] = steps;
+            }
+        }
+        vol = warp_sum_d(vpart) / 6.0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) F += __popc(__ballot_sync(FULL, fdegr[r] > 0));
+        // Every vertex has three faces: V - E + F = 2 with E = 3V/2.
+        if (nlive > 0 && F != nlive / 2 + 2) bad = true;
+        if (__any_sync(FULL, bad)) status = ST_DEGEN;
+    }
+
+    // ---- outputs ----
+    if (status != ST_OK) {
+        if (GEO) {
+            if (lane == 0) P.geo->status = status;
+            return;
+        }
+        if (lane == 0) {
+            uint32_t* list = nullptr;
+            unsigned* count = nullptr;
+            if (status == ST_GUARD || status == ST_DEGEN) {
+                list = P.list_fp64;
+                count = P.list_fp64_count;
+            } else if (status == ST_VCAP || status == ST_PCAP) {
+                list = P.list_cap;
+                count = P.list_cap_count;
+            }
+            if (list) {
+                list[atomicAdd(count, 1u)] = gs;
+                P.status[orig] = ST_PENDING;
+            } else {
+                P.status[orig] = (uint8_t)status;
+                P.vol[orig] = 0.0;
+                P.nface[orig] = 0;
+                atomicAdd(P.fail_count, 1u);
+            }
+        }
+        return;
+    }
+    // compact live face ids, rank faces by id (faces are reported sorted)
+    {
+        int base = 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int p = r * 32 + lane;
+            const unsigned m = __ballot_sync(FULL, fdegr[r] > 0);
+            if (fdegr[r] > 0) S.flist[base + __popc(m & ((1u << lane) - 1u))] = S.pid[p];
+            base += __popc(m);
+        }
+        __syncwarp();
+    }
+    int rank[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        rank[r] = 0;
+        if (fdegr[r] > 0) {
+            const int32_t my = S.pid[r * 32 + lane];
+            for (int q = 0; q < F; ++q) rank[r] += S.flist[q] < my;
+        }
+    }
+    if (GEO) {
+        GeoOut* G = P.geo;
+        // vertices: live slots renumbered in slot order
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if ((C.lm[k] >> lane) & 1u) {
+                int vi = __popc(C.lm[k] & ((1u << lane) - 1u));
+#pragma unroll
+                for (int kk = 0; kk < K; ++kk)
+                    if (kk < k) vi += __popc(C.lm[kk]);
+                const int s = k * 32 + lane;
+                G->verts[3 * vi] = (double)S.vx[s];
+                G->verts[3 * vi + 1] = (double)S.vy[s];
+                G->verts[3 * vi + 2] = (double)S.vz[s];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (fdegr[r] > 0) {
+                S.rank2p[rank[r]] = (uint8_t)(r * 32 + lane);
+                G->face_nbr[rank[r]] = S.pid[r * 32 + lane];
+                G->face_area[rank[r]] = farea[r];
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {
+            int off = 0;
+            for (int q = 0; q < F; ++q) {
+                const int p = S.rank2p[q];
+                G->face_off[q] = off;
+                const int deg = (int)S.fdeg[p];
+                const int start = S.fsta[p];
+                int cur = start;
+                // reversed walk: counter-clockwise seen from outside
+                for (int st = 0; st < deg; ++st) {
+                    int vi = 0;
+                    for (int k = 0; k < K; ++k) {
+                        if ((cur >> 5) == k) vi += __popc(C.lm[k] & ((1u << (cur & 31)) - 1u));
+                        else if ((cur >> 5) > k) vi += __popc(C.lm[k]);
+                    }
+                    G->face_vtx[off + (deg - st) % deg] = vi;
+                    const uint32_t tt = S.tri[cur], aa = S.adj[cur];
+                    const int i = plane_of(tt, 0) == p ? 0 : (plane_of(tt, 1) == p ? 1 : 2);
+                    cur = plane_of(aa, i) % S_t::V;
+                }
+                off += deg;
+            }
+            G->face_off[F] = off;
+            G->nv = nlive;
+            G->nf = F;
+            G->volume = vol;
+            G->status = ST_OK;
+        }
+        return;
+    }
+    unsigned long long fbase = 0;
+    if (lane == 0) fbase = atomicAdd(P.face_cursor, (unsigned long long)F);
+    fbase = __shfl_sync(FULL, fbase, 0);
+    if (fbase + F > P.face_cap) {
+        if (lane == 0) {
+            P.status[orig] = ST_POOL;
+            P.nface[orig] = 0;
+        }
+        return;   // the host sees the face cursor past the capacity and recomputes
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (fdegr[r] > 0) {
+            P.face_nbr[fbase + rank[r]] = S.pid[r * 32 + lane];
+            P.face_area[fbase + rank[r]] = farea[r];
+        }
+    }
+    if (lane == 0) {
+        P.vol[orig] = vol;
+        P.nface[orig] = (uint32_t)F;
+        P.fstart[orig] = fbase;
+        P.status[orig] = ST_OK;
+    }
+}
+
+template <typename T, int K, bool GEO>
+__global__ void k_clip(ClipParams P) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    Smem<T, K>& S = reinterpret_cast<Smem<T, K>*>(smraw)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned w = 0;
+        if (lane == 0) w = atomicAdd(P.cursor, 1u);
+        w = __shfl_sync(FULL, w, 0);
+        const unsigned total = P.work_count ? *P.work_count : P.total;
+        if (w >= total) break;
+        const uint32_t gs = P.work ? P.work[w] : w;
+        run_cell<T, K, GEO>(P, S, gs, lane);
+    }
+}
+
+template <typename T, int K, bool GEO>
+cudaError_t launch_t(const ClipParams& p, int wpb, int blocks, cudaStream_t s) {
+    const size_t sm = sizeof(Smem<T, K>) * (size_t)wpb;
+    auto fn = k_clip<T, K, GEO>;
+    static size_t configured = 0;   // attribute calls stay out of stream capture once set
+    if (sm > configured) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        if (e != cudaSuccess) return e;
+        configured = 100 * 1024;
+    }
+    fn<<<blocks, 32 * wpb, sm, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <typename T, int K, bool GEO>
+int blocks_t(int wpb, int device) {
+    const size_t sm = sizeof(Smem<T, K>) * (size_t)wpb;
+    auto fn = k_clip<T, K, GEO>;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 32 * wpb, sm);
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    if (per < 1) per = 1;
+    return per * nsm;
+}
+
+}  // namespace clipk
+}  // namespace tess

@@ -1,0 +1,342 @@
+// tess_grid.cu -- the binning pass (the GPU form of Celery::reset,
+// celery.rs:253-266): tight bounds, bin sizes, bin histogram, exclusive scan
+// into delimiters, scatter into bin order, gather of sorted positions, and the
+// per-diagram shell table.  All passes are HBM-bound streaming kernels; the
+// integer outputs (bins, delimiters, sorted order) are bit-exact with the
+// reference formulas.
+#include <cfloat>
+#include <cmath>
+
+#include "tess_internal.cuh"
+
+namespace tess {
+namespace {
+
+constexpr int kBoundsThreads = 256;
+
+__device__ __forceinline__ double warp_min(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// CeleryBounds::new (celery.rs:81-125): per-chunk min/max, merged with
+// order-preserving 64-bit atomics.  Non-finite inputs raise error_flag.
+__global__ void __launch_bounds__(kBoundsThreads) k_bounds(GridBuffers g) {
+    __shared__ double red[6][kBoundsThreads / 32];
+    for (uint32_t c = blockIdx.x; c < g.nchunks; c += gridDim.x) {
+        const uint32_t d = g.chunk_diag[c];
+        const uint32_t beg = g.chunk_start[c];
+        const DiagDesc& D = g.diags[d];
+        const uint32_t end = min(beg + kChunk, D.pt_base + D.n);
+        double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX};
+        double mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+        bool bad = false;
+        for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
+            for (int a = 0; a < 3; ++a) {
+                double v = g.xyz[3ull * i + a];
+                bad |= !isfinite(v);
+                mn[a] = fmin(mn[a], v);
+                mx[a] = fmax(mx[a], v);
+            }
+        }
+        if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(g.error_flag, 1);
+        const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+        for (int a = 0; a < 3; ++a) {
+            double lo = warp_min(mn[a]), hi = warp_max(mx[a]);
+            if (l == 0) { red[a][w] = lo; red[3 + a][w] = hi; }
+        }
+        __syncthreads();
+        if (threadIdx.x < 6) {
+            const int a = threadIdx.x;
+            double v = red[a][0];
+            for (int k = 1; k < kBoundsThreads / 32; ++k) v = a < 3 ? fmin(v, red[a][k]) : fmax(v, red[a][k]);
+            unsigned long long e = ord_enc(v);
+            if (a < 3) atomicMin(&g.bounds[6 * d + a], e);
+            else atomicMax(&g.bounds[6 * d + a], e);
+        }
+        __syncthreads();
+    }
+}
+
+// CeleryCellInfo::new (celery.rs:153-181) from the bounds and the host's cpd.
+__global__ void k_grid_params(GridBuffers g) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= g.ndiag) return;
+    DiagDesc& D = g.diags[d];
+    const double c = (double)D.cpd;
+    double m = DBL_MAX;
+    for (int a = 0; a < 3; ++a) {
+        const double lo = ord_dec(g.bounds[6 * d + a]);
+        const double hi = ord_dec(g.bounds[6 * d + 3 + a]);
+        D.glo[a] = lo;
+        D.ghi[a] = hi;
+        const double ext = __dsub_rn(hi, lo);
+        D.size[a] = __ddiv_rn(ext, c);
+        D.inv[a] = __ddiv_rn(c, ext);
+        if (D.size[a] > 0.0) m = fmin(m, D.size[a]);
+    }
+    // Table extent: every offset whose key is <= (gaps * m)^2 has all gap
+    // counts <= gaps, hence |offset| <= gaps + 1 on every axis.
+    int cheb = g.table_gaps + 1;
+    if (cheb > D.cpd - 1) cheb = D.cpd - 1;
+    if (cheb < 0) cheb = 0;
+    D.cheb = cheb;
+    if (m == DBL_MAX) {          // every point identical: only the own bin holds points
+        D.min_size = 0.0;
+        D.tab_kmax = INFINITY;
+    } else {
+        D.min_size = m;
+        const int gaps = cheb - 1;
+        D.tab_kmax = (cheb >= D.cpd - 1) ? (double)INFINITY
+                                         : __dmul_rn(__dmul_rn((double)gaps, m), __dmul_rn((double)gaps, m));
+    }
+}
+
+// get_cells (celery.rs:342-354) + histogram.  rank = arrival order in the bin.
+__global__ void k_bin_count(GridBuffers g) {
+    for (uint32_t c = blockIdx.x; c < g.nchunks; c += gridDim.x) {
+        const uint32_t d = g.chunk_diag[c];
+        const uint32_t beg = g.chunk_start[c];
+        const DiagDesc& D = g.diags[d];
+        const uint32_t end = min(beg + kChunk, D.pt_base + D.n);
+        const int cpd = D.cpd;
+        for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
+            const double x = g.xyz[3ull * i], y = g.xyz[3ull * i + 1], z = g.xyz[3ull * i + 2];
+            const int bx = axis_index(x, D.glo[0], D.ghi[0], D.inv[0], cpd);
+            const int by = axis_index(y, D.glo[1], D.ghi[1], D.inv[1], cpd);
+            const int bz = axis_index(z, D.glo[2], D.ghi[2], D.inv[2], cpd);
+            // get_cell_from_indices, celery.rs:317-325
+            const uint64_t b = D.bin_base + ((uint64_t)bx * cpd + by) * cpd + bz;
+            g.bin[i] = (uint32_t)b;
+            g.rank[i] = atomicAdd(&g.delims[b], 1u);
+        }
+    }
+}
+
+// ---- exclusive scan of the bin counts -> delimiters (celery.rs:372-414) ----
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+    const int l = threadIdx.x & 31;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (l >= o) v += t;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan of kScanThreads values; returns the block total.
+__device__ uint32_t block_excl_scan(uint32_t v, uint32_t* out, uint32_t* sh) {
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    uint32_t inc = warp_incl_scan(v);
+    if (l == 31) sh[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0;
+        uint32_t si = warp_incl_scan(s);
+        sh[l] = si - s;
+        if (l == 31) sh[32] = si;
+    }
+    __syncthreads();
+    *out = inc - v + sh[w];
+    uint32_t total = sh[32];
+    __syncthreads();
+    return total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_partial(uint32_t* data, uint64_t n, uint32_t* sums) {
+    __shared__ uint32_t sh[33];
+    const uint64_t base = (uint64_t)blockIdx.x * kScanThreads * kScanItems + (uint64_t)threadIdx.x * kScanItems;
+    uint32_t s = 0;
+    for (int k = 0; k < kScanItems; ++k) s += (base + k < n) ? data[base + k] : 0u;
+    uint32_t ex;
+    uint32_t tot = block_excl_scan(s, &ex, sh);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_sums(uint32_t* sums, uint32_t nblocks) {
+    __shared__ uint32_t sh[33];
+    uint32_t carry = 0;
+    for (uint32_t b0 = 0; b0 < nblocks; b0 += kScanThreads) {
+        const uint32_t b = b0 + threadIdx.x;
+        uint32_t v = b < nblocks ? sums[b] : 0u;
+        uint32_t ex;
+        uint32_t tot = block_excl_scan(v, &ex, sh);
+        if (b < nblocks) sums[b] = carry + ex;
+        carry += tot;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_final(uint32_t* data, uint64_t n, const uint32_t* sums) {
+    __shared__ uint32_t sh[33];
+    const uint64_t base = (uint64_t)blockIdx.x * kScanThreads * kScanItems + (uint64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = (base + k < n) ? data[base + k] : 0u;
+        s += v[k];
+    }
+    uint32_t ex;
+    block_excl_scan(s, &ex, sh);
+    uint32_t run = sums[blockIdx.x] + ex;
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) data[base + k] = run;
+        run += v[k];
+    }
+}
+
+// get_sorted_indices (celery.rs:357-369): counting-sort scatter.
+__global__ void k_scatter(GridBuffers g) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.total) return;
+    g.sorted[g.delims[g.bin[i]] + g.rank[i]] = i;
+}
+
+// Within-bin order ascending by input index (deterministic; the reference's
+// sort_unstable_by leaves it unspecified).  Bins hold ~1.25 points.
+__global__ void k_bin_order(GridBuffers g) {
+    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= g.total_bins) return;
+    const uint32_t beg = g.delims[b], end = g.delims[b + 1];
+    if (end - beg < 2) return;
+    for (uint32_t s = beg + 1; s < end; ++s) {
+        uint32_t v = g.sorted[s];
+        uint32_t t = s;
+        while (t > beg && g.sorted[t - 1] > v) {
+            g.sorted[t] = g.sorted[t - 1];
+            --t;
+        }
+        g.sorted[t] = v;
+    }
+}
+
+// Positions (and groups) in sorted order, SoA for coalesced candidate loads.
+__global__ void k_gather(GridBuffers g) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.total) return;
+    const uint32_t i = g.sorted[s];
+    g.inv[i] = s;
+    g.spx[s] = g.xyz[3ull * i];
+    g.spy[s] = g.xyz[3ull * i + 1];
+    g.spz[s] = g.xyz[3ull * i + 2];
+    if (g.sgroup) g.sgroup[s] = g.groups[i];
+}
+
+// ---- shell table (get_search_order, celery.rs:418-679) ----
+// One block per diagram: every offset within Chebyshev radius `cheb` whose key
+// is <= tab_kmax, sorted by (key, i, j, k) with a bitonic sort in shared memory.
+constexpr int kTabThreads = 1024;
+
+__global__ void __launch_bounds__(kTabThreads) k_table(GridBuffers g) {
+    __shared__ unsigned long long skey[kMaxTable];
+    __shared__ uint16_t sidx[kMaxTable];
+    __shared__ unsigned int count;
+    const int d = blockIdx.x;
+    DiagDesc& D = g.diags[d];
+    const int c = D.cheb;
+    const int side = 2 * c + 1;
+    const int total = side * side * side;
+    if (threadIdx.x == 0) count = 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int i = t / (side * side) - c;
+        const int j = (t / side) % side - c;
+        const int k = t % side - c;
+        const double key = gap_key(D.size, i, j, k);
+        if (key <= D.tab_kmax) {
+            unsigned int slot = atomicAdd(&count, 1u);
+            if (slot < (unsigned)kMaxTable) {
+                // keys >= 0 order as their bit patterns; self (-1) sorts first
+                skey[slot] = key < 0.0 ? 0ull : (unsigned long long)__double_as_longlong(key) + 1ull;
+                sidx[slot] = (uint16_t)t;   // t orders (i, j, k) lexicographically
+            }
+        }
+    }
+    __syncthreads();
+    const unsigned cap = min((unsigned)kMaxTable, D.tab_cap);
+    if (count > cap && threadIdx.x == 0) atomicExch(g.error_flag, 2);
+    const int m = (int)min(count, cap);
+    int p2 = 1;
+    while (p2 < m) p2 <<= 1;
+    for (int t = m + threadIdx.x; t < p2; t += blockDim.x) {
+        skey[t] = ~0ull;
+        sidx[t] = 0xFFFF;
+    }
+    __syncthreads();
+    for (int k2 = 2; k2 <= p2; k2 <<= 1) {
+        for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
+            for (int t = threadIdx.x; t < p2; t += blockDim.x) {
+                const int u = t ^ j2;
+                if (u > t) {
+                    const bool up = (t & k2) == 0;
+                    const unsigned long long ka = skey[t], kb = skey[u];
+                    const uint16_t ia = sidx[t], ib = sidx[u];
+                    const bool gt = (ka > kb) || (ka == kb && ia > ib);
+                    if (gt == up) {
+                        skey[t] = kb; skey[u] = ka;
+                        sidx[t] = ib; sidx[u] = ia;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+        const int e = sidx[t];
+        const int i = e / (side * side) - c;
+        const int j = (e / side) % side - c;
+        const int k = e % side - c;
+        const double key = gap_key(D.size, i, j, k);
+        TabEntry te;
+        te.key = key < 0.0 ? -1.0f : __double2float_rz(key);
+        te.i = (int8_t)i;
+        te.j = (int8_t)j;
+        te.k = (int8_t)k;
+        te.pad = 0;
+        g.table[D.tab_base + t] = te;
+    }
+    if (threadIdx.x == 0) D.tab_len = (uint32_t)m;
+}
+
+}  // namespace
+
+size_t scan_tmp_words(uint64_t nitems) {
+    const uint64_t per = (uint64_t)kScanThreads * kScanItems;
+    return (size_t)((nitems + per - 1) / per) + 1;
+}
+
+namespace {
+__global__ void k_bounds_init(unsigned long long* b, int ndiag) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < 6 * ndiag) b[t] = (t % 6) < 3 ? ~0ull : 0ull;
+}
+}  // namespace
+
+// Binning pass: bounds -> grid parameters -> shell tables -> histogram ->
+// scan -> scatter -> within-bin order -> gather.  A fixed launch sequence
+// (no host synchronisation), so it can be captured in a CUDA graph.
+cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s) {
+    const int ndiag = g.ndiag;
+    k_bounds_init<<<(6 * ndiag + 255) / 256, 256, 0, s>>>(g.bounds, ndiag);
+    cudaMemsetAsync(g.delims, 0, sizeof(uint32_t) * (g.total_bins + 1), s);
+    cudaMemsetAsync(g.error_flag, 0, sizeof(int), s);
+    const int cblocks = (int)(g.nchunks < 4096u ? g.nchunks : 4096u);
+    k_bounds<<<cblocks, kBoundsThreads, 0, s>>>(g);
+    k_grid_params<<<(ndiag + 127) / 128, 128, 0, s>>>(g);
+    k_table<<<ndiag, kTabThreads, 0, s>>>(g);
+    k_bin_count<<<cblocks, 256, 0, s>>>(g);
+    const uint64_t nscan = g.total_bins + 1;
+    const uint64_t per = (uint64_t)kScanThreads * kScanItems;
+    const uint32_t nblk = (uint32_t)((nscan + per - 1) / per);
+    k_scan_partial<<<nblk, kScanThreads, 0, s>>>(g.delims, nscan, g.scan_tmp);
+    k_scan_sums<<<1, kScanThreads, 0, s>>>(g.scan_tmp, nblk);
+    k_scan_final<<<nblk, kScanThreads, 0, s>>>(g.delims, nscan, g.scan_tmp);
+    k_scatter<<<(g.total + 255) / 256, 256, 0, s>>>(g);
+    k_bin_order<<<(unsigned)((g.total_bins + 255) / 256), 256, 0, s>>>(g);
+    k_gather<<<(g.total + 255) / 256, 256, 0, s>>>(g);
+    return cudaGetLastError();
+}
+
+}  // namespace tess

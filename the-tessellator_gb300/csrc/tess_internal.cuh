@@ -1,0 +1,202 @@
+// tess_internal.cuh -- device data layout shared by the binning pass, the
+// clipping kernels and the host driver of libtessgpu.so (sm_103a).
+//
+// HBM layout of one set of diagrams (a single Diagram is a set of one):
+//   points   xyz[3 * total]            FP64 AoS, concatenated diagram by diagram
+//   bins     bin[total], rank[total]    global bin id and arrival rank per point
+//   grid     delims[total_bins + 1]     CSR offsets of the bin-sorted order
+//   sorted   sorted[total]              sorted position -> point (concatenated index)
+//            spx/spy/spz[total]         FP64 positions in sorted order (SoA)
+//            sgroup[total]              group ids in sorted order (optional)
+//   table    tab[...]                   per-diagram shell table (sorted offsets)
+//   results  vol[total], nface[total], fstart[total], status[total]  (point order)
+//            face_nbr[cap], face_area[cap]   face pool, filled by atomic allocation
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tess {
+
+constexpr double kTolerance = 1e-12;        // polyhedron.rs:221-223
+constexpr double kStopMargin = 1.0 + 1e-5;  // slack on the security-radius test
+constexpr int kMaxTable = 4096;             // shell-table entries per diagram (sort capacity)
+
+// Per-cell status codes written by the clipping kernels.
+enum CellStatus : uint8_t {
+    ST_OK = 0,
+    ST_GUARD = 1,       // FP32 plane-side test inside the guard band -> FP64 re-run
+    ST_VCAP = 2,        // vertex capacity exceeded -> larger capacity re-run
+    ST_PCAP = 3,        // face (plane) capacity exceeded -> larger capacity re-run
+    ST_DEGEN = 4,       // inconsistent topology (degenerate input) -> FP64 re-run / error
+    ST_POOL = 5,        // face pool full -> host grows the pool
+    ST_PENDING = 255    // not computed yet
+};
+
+// One diagram as the kernels see it.  Filled partly by the host (counts,
+// bases, box) and partly on the device (bounds, bin sizes, table length).
+struct DiagDesc {
+    double glo[3], ghi[3];   // CeleryBounds (celery.rs:81-125), tight point bounds
+    double size[3];          // x/y/z_cell_size (celery.rs:165-167)
+    double inv[3];           // x/y/z_inverse_cell_size (celery.rs:169-171)
+    double blo[3], bhi[3];   // container box (walls)
+    double tab_kmax;         // every offset with key <= tab_kmax is in the table
+    double min_size;         // smallest nonzero bin side
+    uint64_t bin_base;       // first global bin of this diagram
+    uint64_t tab_base;       // first table entry of this diagram
+    uint32_t pt_base;        // first point (concatenated order == sorted order base)
+    uint32_t n;              // points
+    uint32_t tab_len;        // table entries (device-written)
+    uint32_t tab_cap;        // table capacity reserved by the host
+    int32_t cpd;             // cells_per_dimension (host, glibc cbrt)
+    int32_t cheb;            // Chebyshev radius enumerated into the table
+};
+
+// Shell-table entry: a bin offset and its search-order key (celery.rs:423-427)
+// rounded toward zero to FP32 so the stop test stays conservative.
+struct TabEntry {
+    float key;
+    int8_t i, j, k, pad;
+};
+
+// Output of one cell's full geometry (single-cell queries); the leading
+// fields mirror tess_cell_geometry of the C ABI.
+struct GeoOut {
+    double volume;
+    int32_t nv, nf;
+    double verts[3 * 256];          // site-relative vertex positions
+    int32_t face_nbr[256];
+    double face_area[256];
+    int32_t face_off[257];          // offsets into face_vtx
+    int32_t face_vtx[3 * 256];      // vertex indices, CCW seen from outside
+    int32_t status;
+};
+
+// Order-preserving map of doubles onto uint64 (for atomicMin/atomicMax).
+__device__ __forceinline__ unsigned long long ord_enc(double v) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ord_dec(unsigned long long e) {
+    unsigned long long b = (e >> 63) ? (e & 0x7FFFFFFFFFFFFFFFull) : ~e;
+    return __longlong_as_double((long long)b);
+}
+
+// get_{x,y,z}_cell_index (celery.rs:269-314): x >= max -> cpd-1, else
+// min(trunc((x - min) * inv), cpd-1), with `as usize` saturating at 0 for
+// negative and NaN values.  Exact FP64 multiply, no FMA.
+__device__ __forceinline__ int axis_index(double x, double lo, double hi, double inv, int cpd) {
+    if (x >= hi) return cpd - 1;
+    double v = __dmul_rn(__dsub_rn(x, lo), inv);
+    if (!(v > 0.0)) return 0;
+    if (v >= (double)(cpd - 1)) return cpd - 1;
+    return (int)v;
+}
+
+// Search-order key of a bin offset (celery.rs:423-427 on the gap counts,
+// celery.rs:447-639), self = -1 (celery.rs:438-443).  Exact FP64, no FMA.
+__device__ __forceinline__ double gap_key(const double size[3], int i, int j, int k) {
+    if (i == 0 && j == 0 && k == 0) return -1.0;
+    int gi = i < 0 ? -i - 1 : (i > 0 ? i - 1 : 0);
+    int gj = j < 0 ? -j - 1 : (j > 0 ? j - 1 : 0);
+    int gk = k < 0 ? -k - 1 : (k > 0 ? k - 1 : 0);
+    double a = __dmul_rn((double)gi, size[0]);
+    double b = __dmul_rn((double)gj, size[1]);
+    double c = __dmul_rn((double)gk, size[2]);
+    return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+}
+
+// ---- launchers (tess_grid.cu) ----
+struct GridBuffers {
+    const double* xyz;          // concatenated points, AoS
+    const uint32_t* groups;     // point groups or null
+    DiagDesc* diags;
+    int ndiag;
+    uint32_t total;             // total points
+    uint64_t total_bins;
+    const uint32_t* chunk_diag; // per 8192-point chunk: diagram id
+    const uint32_t* chunk_start;
+    uint32_t nchunks;
+    unsigned long long* bounds; // 6 per diagram (encoded)
+    uint32_t* bin;
+    uint32_t* rank;
+    uint32_t* delims;           // total_bins + 1
+    uint32_t* scan_tmp;         // block sums
+    uint32_t* sorted;
+    uint32_t* inv;              // point -> sorted position
+    double* spx;
+    double* spy;
+    double* spz;
+    uint32_t* sgroup;           // null when groups is null
+    TabEntry* table;
+    int table_gaps;
+    int* error_flag;            // set when an input coordinate is not finite
+};
+constexpr uint32_t kChunk = 8192;
+constexpr int kScanItems = 8;       // items per thread in the scan
+constexpr int kScanThreads = 1024;
+
+cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s);
+size_t scan_tmp_words(uint64_t nitems);
+
+// ---- launchers (tess_clip.cu) ----
+struct ClipParams {
+    const DiagDesc* diags;
+    int ndiag;
+    const double* spx;
+    const double* spy;
+    const double* spz;
+    const uint32_t* sorted;
+    const uint32_t* delims;
+    const uint32_t* sgroup;
+    const TabEntry* table;
+    // work: sorted positions to process
+    const uint32_t* work;          // null: 0 .. total-1
+    const uint32_t* work_count;    // null: total
+    uint32_t total;
+    unsigned int* cursor;          // work cursor (zeroed before launch)
+    // results, indexed by point (concatenated original order)
+    double* vol;
+    uint32_t* nface;
+    uint64_t* fstart;
+    uint8_t* status;
+    int32_t* face_nbr;
+    double* face_area;
+    unsigned long long* face_cursor;
+    uint64_t face_cap;
+    // routing of failed cells
+    uint32_t* list_fp64;          // guard / degenerate cells (FP32 pass) or null
+    unsigned int* list_fp64_count;
+    uint32_t* list_cap;           // capacity overflow cells or null
+    unsigned int* list_cap_count;
+    unsigned int* fail_count;     // cells left with an error status
+    // options
+    double search_radius;         // < 0: none
+    int64_t target_group;         // < 0: none
+    float guard_rel;
+    float verify_rel;
+    // single-cell geometry output (queries); null for bulk runs
+    GeoOut* geo;
+    int at_point;                 // 1: site = point[] below, not a diagram point
+    double point[3];
+    int box_override;             // 1: walls from box[] instead of the diagram's box
+    double box[6];                // lo xyz, hi xyz
+};
+
+cudaError_t launch_clip_f32(const ClipParams& p, int slots, int wpb, int blocks, cudaStream_t s);
+cudaError_t launch_clip_f64(const ClipParams& p, int slots, int wpb, int blocks, cudaStream_t s);
+int clip_blocks_f32(int slots, int wpb, int device);
+int clip_blocks_f64(int slots, int wpb, int device);
+// precision: 0 FP64, 1 FP32.  slots: 2, 4 or 8.
+cudaError_t launch_clip(const ClipParams& p, int precision, int slots, int warps_per_block,
+                        int blocks, cudaStream_t s);
+int clip_blocks_for(int precision, int slots, int warps_per_block, int device);
+// CSR offsets (3 launches) and the gather into them (1 launch).
+cudaError_t launch_csr_offsets(const uint32_t* nface, uint32_t n, uint64_t* offs, uint64_t* scan_tmp,
+                               cudaStream_t s);
+cudaError_t launch_csr_gather(const uint32_t* nface, const uint64_t* fstart, const int32_t* face_nbr,
+                              const double* face_area, uint32_t n, const uint64_t* offs, int32_t* nbr_out,
+                              double* area_out, cudaStream_t s);
+size_t csr_tmp_words(uint32_t n);
+
+}  // namespace tess

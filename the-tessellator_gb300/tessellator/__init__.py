@@ -1,0 +1,390 @@
+"""tessellator: GB300-native Voronoi cells behind the API of
+mcomstock/the-tessellator (src/interface.rs).
+
+The classes mirror the reference's public types:
+
+    Polyhedron   the container box a caller hands to get_cell_at_index
+                 (polyhedron.rs:226-244, Polyhedron::new)
+    Diagram      point set + GPU bin grid (interface.rs:25-84; the reference
+                 has no public constructor, this one takes points and a box)
+    Cell         get_cell_at_index / get_cell_at_particle + compute_voronoi_cell
+                 (interface.rs:186-334)
+    VoronoiFace  compute_vertices / compute_area / compute_neighbor
+                 (interface.rs:393-416)
+
+plus the bulk path the GPU is built for: ``Diagram.compute_all`` with
+``volumes()`` and ``neighbors_csr()``, and ``Batch`` for many diagrams in one
+CUDA-graph launch.  Every computation runs in libtessgpu.so on the GPU; there
+is no CPU fallback.
+
+Conventions: indices are the caller's original indices; box faces report
+neighbour ids -1 (x_min), -2 (x_max), -3 (y_min), -4 (y_max), -5 (z_min),
+-6 (z_max); a cell's faces come sorted by neighbour id; vertices are relative
+to the cell's site (the reference leaves its polyhedron translated by
+-position, interface.rs:266).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Optional
+
+import numpy as np
+
+from ._capi import (FLAG_TIMING, PRECISION_FP32_GUARD, PRECISION_FP64, CellGeometry, Config, Stats,
+                    TessError, check, default_config, last_error, lib)
+
+__all__ = ["Polyhedron", "Diagram", "Cell", "VoronoiFace", "Batch", "TessError", "Config",
+           "default_config", "PRECISION_FP64", "PRECISION_FP32_GUARD", "FLAG_TIMING", "lib",
+           "last_error"]
+
+_PREC = {"fp64": PRECISION_FP64, "fp32": PRECISION_FP32_GUARD, "fp32_guard": PRECISION_FP32_GUARD,
+         PRECISION_FP64: PRECISION_FP64, PRECISION_FP32_GUARD: PRECISION_FP32_GUARD}
+
+
+def _prec(p) -> int:
+    try:
+        return _PREC[p]
+    except KeyError:
+        raise ValueError(f"unknown precision {p!r} (use 'fp64' or 'fp32')") from None
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _radius(r: Optional[float]) -> float:
+    return -1.0 if r is None else float(r)
+
+
+def _group(g: Optional[int]) -> int:
+    return -1 if g is None else int(g)
+
+
+class Polyhedron:
+    """The axis-aligned container box (Polyhedron::new, polyhedron.rs:226-244)."""
+
+    def __init__(self, x_min, y_min, z_min, x_max, y_max, z_max):
+        self.lo = np.array([x_min, y_min, z_min], dtype=np.float64)
+        self.hi = np.array([x_max, y_max, z_max], dtype=np.float64)
+
+    @classmethod
+    def new(cls, x_min, y_min, z_min, x_max, y_max, z_max) -> "Polyhedron":
+        return cls(x_min, y_min, z_min, x_max, y_max, z_max)
+
+
+class Diagram:
+    """Points, groups and the GPU bin grid (Diagram, interface.rs:25-84).
+
+    ``points``: (n, 3) float64.  ``container``: a Polyhedron box, or None for
+    the reference's Diagram bounding box (starts at the origin and grows to
+    contain every point).  ``device_ptr``: build from n x 3 doubles already in
+    device memory (an integer address) instead of ``points``.
+    """
+
+    def __init__(self, points=None, groups=None, container: Optional[Polyhedron] = None,
+                 config: Optional[Config] = None, device_ptr: Optional[int] = None, n: Optional[int] = None):
+        L = lib()
+        self._h = C.c_void_p()
+        cfg = config if config is not None else default_config()
+        self.config = cfg
+        g = None if groups is None else np.ascontiguousarray(groups, dtype=np.uint32)
+        lo = None if container is None else np.ascontiguousarray(container.lo)
+        hi = None if container is None else np.ascontiguousarray(container.hi)
+        gp = None if g is None else g.ctypes.data_as(C.POINTER(C.c_uint32))
+        lp = None if lo is None else _dp(lo)
+        hp = None if hi is None else _dp(hi)
+        if device_ptr is not None:
+            if n is None:
+                raise ValueError("n is required with device_ptr")
+            self.n = int(n)
+            check(L.tess_diagram_create_device(C.c_void_p(device_ptr), self.n, gp, lp, hp, C.byref(cfg),
+                                               C.byref(self._h)))
+        else:
+            pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+            self.n = len(pts)
+            if g is not None and len(g) != self.n:
+                raise ValueError("groups must have one entry per point")
+            check(L.tess_diagram_create(_dp(pts), self.n, gp, lp, hp, C.byref(cfg), C.byref(self._h)))
+        self.container = container
+
+    # ---- lifetime ----
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().tess_diagram_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return self.n
+
+    # ---- bulk path ----
+    def rebuild(self):
+        """Re-bin the points held on the device (Celery::reset, celery.rs:253-266)."""
+        check(lib().tess_diagram_rebuild(self._h))
+
+    def update_points(self, points=None, device_ptr: Optional[int] = None):
+        """Replace the points (same count) and re-bin them."""
+        if device_ptr is not None:
+            check(lib().tess_diagram_update_points(self._h, C.c_void_p(device_ptr), 1))
+        else:
+            pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+            if len(pts) != self.n:
+                raise ValueError("update_points keeps the point count")
+            check(lib().tess_diagram_update_points(self._h, C.c_void_p(pts.ctypes.data), 0))
+
+    def celery(self):
+        """The bin grid's public fields (celery.rs:196-217):
+        (cells[n], sorted_indices[n], delimiters[cpd^3 + 1])."""
+        cpd, _ = self.grid()
+        cells = np.empty(self.n, dtype=np.uint32)
+        srt = np.empty(self.n, dtype=np.uint32)
+        dl = np.empty(cpd ** 3 + 1, dtype=np.uint32)
+        u = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint32))
+        check(lib().tess_diagram_celery(self._h, u(cells), u(srt), u(dl)))
+        return cells, srt, dl
+
+    def compute_all(self, precision="fp32", search_radius: Optional[float] = None,
+                    target_group: Optional[int] = None) -> "Diagram":
+        """Every cell: get_cell_at_index(i, ...) + compute_voronoi_cell()."""
+        check(lib().tess_diagram_compute_all(self._h, _prec(precision), _radius(search_radius),
+                                             _group(target_group)))
+        return self
+
+    def volumes(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.float64)
+        check(lib().tess_volumes(self._h, _dp(out)))
+        return out
+
+    def neighbors_csr(self):
+        """(offsets[n+1] uint64, neighbour ids int32, face areas float64)."""
+        L = lib()
+        offs = np.empty(self.n + 1, dtype=np.uint64)
+        total = C.c_size_t(0)
+        check(L.tess_neighbors_csr(self._h, offs.ctypes.data_as(C.POINTER(C.c_uint64)), None, None, 0,
+                                   C.byref(total)))
+        nbr = np.empty(max(total.value, 1), dtype=np.int32)
+        area = np.empty(max(total.value, 1), dtype=np.float64)
+        check(L.tess_neighbors_csr(self._h, None, nbr.ctypes.data_as(C.POINTER(C.c_int32)), _dp(area),
+                                   len(nbr), C.byref(total)))
+        return offs, nbr[:total.value], area[:total.value]
+
+    def results_device(self):
+        """Device addresses (volumes, offsets, neighbour ids, areas, total faces)."""
+        v, o, nb, a = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+        total = C.c_size_t(0)
+        check(lib().tess_results_device(self._h, C.byref(v), C.byref(o), C.byref(nb), C.byref(a),
+                                        C.byref(total)))
+        return v.value, o.value, nb.value, a.value, total.value
+
+    def stats(self) -> dict:
+        s = Stats()
+        check(lib().tess_diagram_stats(self._h, C.byref(s)))
+        return s.as_dict()
+
+    def grid(self):
+        """(cells_per_dimension, bounds {xmin, xmax, ymin, ymax, zmin, zmax})."""
+        cpd = C.c_int64(0)
+        b = np.zeros(6)
+        check(lib().tess_diagram_grid(self._h, C.byref(cpd), _dp(b)))
+        return cpd.value, b
+
+    # ---- per-cell results of the last compute_all ----
+    def cell_volume(self, i: int) -> float:
+        v = C.c_double(0.0)
+        check(lib().tess_cell_volume(self._h, i, C.byref(v)))
+        return v.value
+
+    def cell_faces(self, i: int):
+        """(neighbour ids, areas) of cell i, sorted by id."""
+        L = lib()
+        cnt = C.c_size_t(0)
+        nbr = np.empty(256, dtype=np.int32)
+        area = np.empty(256, dtype=np.float64)
+        check(L.tess_cell_faces(self._h, i, nbr.ctypes.data_as(C.POINTER(C.c_int32)), _dp(area), 256,
+                                C.byref(cnt)))
+        return nbr[:cnt.value].copy(), area[:cnt.value].copy()
+
+    def cell_neighbors(self, i: int) -> np.ndarray:
+        return self.cell_faces(i)[0]
+
+    def cell_vertices(self, i: int) -> np.ndarray:
+        cnt = C.c_size_t(0)
+        buf = np.empty((256, 3), dtype=np.float64)
+        check(lib().tess_cell_vertices(self._h, i, _dp(buf), 256, C.byref(cnt)))
+        return buf[:cnt.value].copy()
+
+    def cell_face_vertices(self, i: int, face: int) -> np.ndarray:
+        cnt = C.c_size_t(0)
+        buf = np.empty((256, 3), dtype=np.float64)
+        check(lib().tess_cell_face_vertices(self._h, i, face, _dp(buf), 256, C.byref(cnt)))
+        return buf[:cnt.value].copy()
+
+    # ---- the reference's per-cell API ----
+    def get_cell_at_index(self, index: int, polyhedron: Optional[Polyhedron] = None,
+                          search_radius: Optional[float] = None, target_group: Optional[int] = None,
+                          precision="fp64") -> "Cell":
+        """Diagram::get_cell_at_index (interface.rs:186-208)."""
+        if not 0 <= index < self.n:
+            raise IndexError(index)
+        return Cell(self, index, None, polyhedron, search_radius, target_group, precision)
+
+    def get_cell_at_particle(self, point, polyhedron: Optional[Polyhedron] = None,
+                             search_radius: Optional[float] = None, target_group: Optional[int] = None,
+                             precision="fp64") -> "Cell":
+        """Diagram::get_cell_at_particle (interface.rs:211-232)."""
+        return Cell(self, None, np.asarray(point, dtype=np.float64), polyhedron, search_radius,
+                    target_group, precision)
+
+
+class Cell:
+    """A Voronoi cell (Cell, interface.rs:237-390)."""
+
+    def __init__(self, diagram: Diagram, index, point, polyhedron, search_radius, target_group, precision):
+        self.diagram = diagram
+        self.index = index
+        self.point = point
+        self.polyhedron = polyhedron
+        self.search_radius = search_radius
+        self.target_group = target_group
+        self.precision = precision
+        self._g: Optional[CellGeometry] = None
+
+    def compute_voronoi_cell(self) -> "Cell":
+        """Cell::compute_voronoi_cell (interface.rs:257-313), on the GPU."""
+        L = lib()
+        g = CellGeometry()
+        lo = hi = None
+        if self.polyhedron is not None:
+            lo = np.ascontiguousarray(self.polyhedron.lo)
+            hi = np.ascontiguousarray(self.polyhedron.hi)
+        lp = None if lo is None else _dp(lo)
+        hp = None if hi is None else _dp(hi)
+        if self.index is not None:
+            st = L.tess_cell_compute(self.diagram._h, self.index, _prec(self.precision),
+                                     _radius(self.search_radius), _group(self.target_group), lp, hp,
+                                     C.byref(g))
+        else:
+            p = np.ascontiguousarray(self.point)
+            st = L.tess_cell_compute_at(self.diagram._h, _dp(p), _prec(self.precision),
+                                        _radius(self.search_radius), _group(self.target_group), lp, hp,
+                                        C.byref(g))
+        check(st)
+        self._g = g
+        return self
+
+    def _geom(self) -> CellGeometry:
+        if self._g is None:
+            self.compute_voronoi_cell()
+        return self._g
+
+    def compute_volume(self) -> float:
+        """Cell::compute_volume (interface.rs:337-339)."""
+        return self._geom().volume
+
+    def compute_neighbors(self) -> List[int]:
+        """Cell::compute_neighbors (interface.rs:342-344); walls are negative ids."""
+        g = self._geom()
+        return [g.face_neighbor[f] for f in range(g.nfaces)]
+
+    def compute_vertices(self) -> np.ndarray:
+        """Cell::compute_vertices (interface.rs:368-370), site-relative."""
+        g = self._geom()
+        return np.ctypeslib.as_array(g.vertices)[: 3 * g.nvertices].reshape(-1, 3).copy()
+
+    def compute_faces(self) -> List["VoronoiFace"]:
+        """Cell::compute_faces (interface.rs:373-384)."""
+        g = self._geom()
+        return [VoronoiFace(self, f) for f in range(g.nfaces)]
+
+    def original_index(self) -> Optional[int]:
+        """Cell::original_index (interface.rs:387-389)."""
+        return self.index
+
+
+class VoronoiFace:
+    """A face of a Voronoi cell (VoronoiFace, interface.rs:393-416)."""
+
+    def __init__(self, cell: Cell, face_index: int):
+        self.cell = cell
+        self.face_index = face_index
+
+    def compute_vertices(self) -> np.ndarray:
+        g = self.cell._geom()
+        b, e = g.face_offset[self.face_index], g.face_offset[self.face_index + 1]
+        verts = np.ctypeslib.as_array(g.vertices)[: 3 * g.nvertices].reshape(-1, 3)
+        idx = [g.face_vertex[t] for t in range(b, e)]
+        return verts[idx].copy()
+
+    def compute_area(self) -> float:
+        return self.cell._geom().face_area[self.face_index]
+
+    def compute_neighbor(self) -> int:
+        return self.cell._geom().face_neighbor[self.face_index]
+
+
+class Batch:
+    """Many independent diagrams computed in one CUDA-graph launch.
+
+    ``points``: (total, 3) float64 concatenated; ``offsets``: ndiag+1 point
+    offsets; ``boxes``: (ndiag, 6) {xlo, ylo, zlo, xhi, yhi, zhi}.
+    """
+
+    def __init__(self, points, offsets, boxes, config: Optional[Config] = None):
+        L = lib()
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+        offs = np.ascontiguousarray(offsets, dtype=np.uint64)
+        bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.float64).reshape(-1, 6))
+        self.n = len(pts)
+        self.ndiag = len(offs) - 1
+        self._h = C.c_void_p()
+        cfg = config if config is not None else default_config()
+        check(L.tess_batch_create(self.ndiag, offs.ctypes.data_as(C.POINTER(C.c_uint64)), _dp(pts), _dp(bx),
+                                  C.byref(cfg), C.byref(self._h)))
+
+    def compute(self, precision="fp32") -> "Batch":
+        check(lib().tess_batch_compute(self._h, _prec(precision)))
+        return self
+
+    def volumes(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.float64)
+        check(lib().tess_batch_volumes(self._h, _dp(out)))
+        return out
+
+    def neighbors_csr(self):
+        L = lib()
+        offs = np.empty(self.n + 1, dtype=np.uint64)
+        total = C.c_size_t(0)
+        check(L.tess_batch_neighbors_csr(self._h, offs.ctypes.data_as(C.POINTER(C.c_uint64)), None, None, 0,
+                                         C.byref(total)))
+        nbr = np.empty(max(total.value, 1), dtype=np.int32)
+        area = np.empty(max(total.value, 1), dtype=np.float64)
+        check(L.tess_batch_neighbors_csr(self._h, None, nbr.ctypes.data_as(C.POINTER(C.c_int32)), _dp(area),
+                                         len(nbr), C.byref(total)))
+        return offs, nbr[:total.value], area[:total.value]
+
+    def stats(self) -> dict:
+        s = Stats()
+        check(lib().tess_batch_stats(self._h, C.byref(s)))
+        return s.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().tess_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
