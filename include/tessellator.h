@@ -93,6 +93,9 @@ typedef struct {
     double ms_rerun;            /* re-run passes                                   */
     double ms_csr;              /* CSR compaction                                  */
     uint64_t launches;          /* kernels launched by this handle so far          */
+    uint64_t rerun_guard;       /* ... of them: a plane test inside the guard band */
+    uint64_t rerun_verify;      /* ... FP32 vertex too far from its FP64 position   */
+    uint64_t rerun_degenerate;  /* ... inconsistent topology                        */
 } tess_stats;
 
 void tess_config_default(tess_config* cfg);

@@ -1,0 +1,97 @@
+"""The C ABI library without a GPU: it loads, exports every function that
+include/tessellator.h declares, and rejects bad arguments with an error
+status (no compute calls are made here)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "tessellator.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tess_[a-z_0-9]+)\s*\(", text)))
+
+
+def exported_symbols(path):
+    import subprocess
+
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True, check=True).stdout
+    return {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+
+
+def test_every_declared_function_is_exported(tess):
+    decl = declared_functions()
+    assert len(decl) >= 25
+    syms = exported_symbols(tess._capi.LIB_PATH)
+    missing = [f for f in decl if f not in syms]
+    assert not missing, missing
+    # the Python binding declares the same set
+    assert sorted(tess._capi.EXPORTS) == decl
+
+
+def test_library_needs_no_gpu_to_load(tess):
+    L = tess.lib()
+    assert L.tess_version().startswith(b"tessellator-gb300")
+
+
+def test_default_config(tess):
+    c = tess.default_config()
+    assert c.bin_density == 1.25          # celery.rs:185-188
+    assert c.slots_per_lane == 2 and c.table_gaps == 8
+    assert 0 < c.guard_rel < 1e-3
+    assert c.stream is None and c.flags == 0
+
+
+def test_argument_errors(tess):
+    L = tess.lib()
+    h = C.c_void_p()
+    st = L.tess_diagram_create(None, 10, None, None, None, None, C.byref(h))
+    assert st == tess._capi.TESS_E_INVALID
+    assert "xyz" in tess.last_error()
+    pts = np.zeros((4, 3))
+    lo = np.array([1.0, 0, 0])
+    hi = np.array([0.0, 1, 1])
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    st = L.tess_diagram_create(dp(pts), 0, None, None, None, None, C.byref(h))
+    assert st == tess._capi.TESS_E_INVALID
+    st = L.tess_diagram_create(dp(pts), 4, None, dp(lo), None, None, C.byref(h))
+    assert st == tess._capi.TESS_E_INVALID
+    assert L.tess_cell_volume(None, 0, None) == tess._capi.TESS_E_INVALID
+    assert L.tess_diagram_compute_all(None, 0, -1.0, -1) == tess._capi.TESS_E_INVALID
+    offs = np.array([0, 5, 5], dtype=np.uint64)
+    st = L.tess_batch_create(2, offs.ctypes.data_as(C.POINTER(C.c_uint64)), dp(np.zeros((5, 3))),
+                             dp(np.zeros((2, 6))), None, C.byref(h))
+    assert st == tess._capi.TESS_E_INVALID   # second diagram empty
+    bad = tess.default_config(slots_per_lane=3)
+    with pytest.raises(tess.TessError) as e:
+        tess.Diagram(np.random.rand(10, 3), config=bad)
+    assert e.value.status in (tess._capi.TESS_E_INVALID, tess._capi.TESS_E_CUDA)
+
+
+def test_fails_loudly_without_a_device(tess):
+    """No CPU fallback: without a CUDA device the constructor reports TESS_E_CUDA."""
+    pytest.importorskip("torch")
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(tess.TessError) as e:
+        tess.Diagram(np.random.rand(10, 3))
+    assert e.value.status == tess._capi.TESS_E_CUDA
+
+
+def test_python_api_mirrors_interface_rs(tess):
+    """The reference's public method names exist on the mirror classes."""
+    for name in ("get_cell_at_index", "get_cell_at_particle"):
+        assert hasattr(tess.Diagram, name)
+    for name in ("compute_voronoi_cell", "compute_volume", "compute_neighbors", "compute_vertices",
+                 "compute_faces", "original_index"):
+        assert hasattr(tess.Cell, name)
+    for name in ("compute_vertices", "compute_area", "compute_neighbor"):
+        assert hasattr(tess.VoronoiFace, name)
+    assert hasattr(tess.Polyhedron, "new")

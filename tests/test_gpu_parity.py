@@ -29,7 +29,7 @@ def compare(prec, gpu, ref, n, check_sum=None):
     scale = np.repeat(cellmax, counts[counts > 0])
     assert np.all(np.abs(area - ra) <= AREA_TOL[prec] * scale)
     if check_sum is not None:
-        assert abs(vol.sum() - check_sum) <= 1e-9 * check_sum
+        assert abs(vol.sum() - check_sum) <= (1e-11 if prec == "fp64" else 1e-6) * check_sum
 
 
 def gpu_all(T, pts, prec, container=None, config=None, **kw):

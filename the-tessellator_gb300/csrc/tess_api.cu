@@ -66,7 +66,7 @@ int64_t cells_per_dim(uint64_t n, double density) {
     return (int64_t)v + 1;
 }
 
-enum { L_FP64 = 0, L_CAP1 = 1, L_CAP2 = 2, L_CAP64A = 3, L_CAP64B = 4, L_COUNT = 5, L_FAIL = 10 };
+enum { L_FP64 = 0, L_CAP1 = 1, L_CAP2 = 2, L_CAP64A = 3, L_CAP64B = 4, L_COUNT = 5, L_FAIL = 6, L_REASON = 8 };
 // Kernels launched by one binning pass (launch_grid_build).
 constexpr uint64_t kGridLaunches = 11;
 
@@ -161,7 +161,7 @@ struct Engine {
     }
     int wpb_for(int precision, int slots) const {
         int w = cfg.warps_per_block;
-        if (slots >= 8) w = std::min(w, precision == 1 ? 4 : 2);
+        if (slots >= 8) w = std::min(w, 2);
         else if (slots >= 4) w = std::min(w, 4);
         return std::max(1, w);
     }
@@ -397,6 +397,7 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         p.list_cap = lcap;
         p.list_cap_count = ccap;
         p.fail_count = cnt + L_FAIL;
+        p.reasons = cnt + L_REASON;
         CU(launch_clip(p, prec, slots, E.wpb_for(prec, slots), E.blocks(prec, slots), E.stream));
         E.launches += 1;
         return TESS_OK;
@@ -488,6 +489,9 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
         E.last_group = group;
         const uint64_t failed = counts[L_FAIL];
         E.stats.failed = failed;
+        E.stats.rerun_guard = counts[L_REASON + ST_GUARD];
+        E.stats.rerun_verify = counts[L_REASON + ST_VERIFY];
+        E.stats.rerun_degenerate = counts[L_REASON + ST_DEGEN];
         if (failed) return fail(TESS_E_OVERFLOW, "%llu cells could not be computed", (unsigned long long)failed);
         return TESS_OK;
     }
@@ -1004,6 +1008,9 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
     E.stats.rerun_fp64 = prec == 1 ? counts[L_FP64] : 0;
     E.stats.rerun_capacity = (uint64_t)counts[L_CAP1] + counts[L_CAP2] + counts[L_CAP64A] + counts[L_CAP64B];
     E.stats.failed = counts[L_FAIL];
+    E.stats.rerun_guard = counts[L_REASON + ST_GUARD];
+    E.stats.rerun_verify = counts[L_REASON + ST_VERIFY];
+    E.stats.rerun_degenerate = counts[L_REASON + ST_DEGEN];
     E.computed = true;
     E.csr_valid = false;
     E.last_precision = prec;

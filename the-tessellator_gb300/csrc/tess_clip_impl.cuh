@@ -58,6 +58,7 @@ struct Smem {
     T px[P], py[P], pz[P], pd[P];     // plane: unit normal, offset
     T vx[V], vy[V], vz[V], vsd[V];    // vertex mirror, signed distances
     int32_t pid[P];                   // neighbour id (local original index) or wall code
+    uint32_t psrc[P];                 // sorted index of the point that made the plane
     uint32_t tri[V];                  // planes a | b << 8 | c << 16
     uint32_t adj[V];                  // neighbours n0 | n1 << 8 | n2 << 16
     uint32_t fdeg[P];                 // finalize: live vertices per face
@@ -66,6 +67,12 @@ struct Smem {
     uint8_t fsta[P];                  // finalize: one vertex of each face
     uint8_t mapf[P], maps[P];         // new-vertex ring maps
     uint8_t rank2p[P];                // geometry output: rank -> plane
+    // FP32 form only: FP64 face planes {n, h} (n.x = h) and their distance
+    // from the site, and per-vertex FP32 corrections to the FP64 position.
+    static constexpr int PF = sizeof(T) == 4 ? P : 1;
+    static constexpr int VF = sizeof(T) == 4 ? V : 1;
+    double qx[PF], qy[PF], qz[PF], qh[PF], qdist[PF];
+    float dx[VF], dy[VF], dz[VF];
 };
 
 __device__ __forceinline__ unsigned warp_incl_scan_u(unsigned v, int lane) {
@@ -160,6 +167,9 @@ __device__ __forceinline__ void bisector(double rx, double ry, double rz, double
     off = nx * (rx * 0.5) + ny * (ry * 0.5) + nz * (rz * 0.5);
 }
 
+__device__ __forceinline__ float round_up_f(float x) { return x; }
+__device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
+
 template <typename T, int K>
 struct CellRegs {
     T vx[K], vy[K], vz[K];
@@ -170,8 +180,8 @@ struct CellRegs {
 // Clip the cell by {x : n.x - off <= 0}.  Returns 1 when vertices were cut
 // off, 0 when nothing was Outside, or -status.
 template <typename T, int K, bool GUARD>
-__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, int32_t id, T guard,
-                   int lane) {
+__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, int32_t id, uint32_t src,
+                   T guard, int lane) {
     using S_t = Smem<T, K>;
     T sd[K];
     uint32_t om[K];
@@ -334,6 +344,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, in
         S.pz[f] = nz;
         S.pd[f] = off;
         S.pid[f] = id;
+        S.psrc[f] = src;
     }
     C.np = f + 1;
     __syncwarp();
@@ -505,7 +516,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 T nx, ny, nz, off;
                 bisector(cx, cy, cz, c2, nx, ny, nz, off);
                 const int32_t id = (int32_t)(P.sorted[cj] - D.pt_base);
-                const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, id, guard, lane);
+                const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, id, cj, guard, lane);
                 if (r < 0) return -r;
                 if (r > 0) {
                     R2 = live_r2(C, lane);
@@ -527,7 +538,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     bool phase2 = false;
     uint32_t t = 0;
     for (;;) {
-        const double thr = 4.0 * (double)R2 * kStopMargin;
+        // The table key is rounded toward zero and the threshold up, so
+        // stopping on key >= thr never drops a bin that could hold a cutter.
+        const float thr = round_up_f((T)4 * R2 * (T)kStopMargin);
         const uint32_t idx = t + lane;
         bool stop = true;
         int oi = 0, oj = 0, ok = 0;
@@ -536,8 +549,8 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             oi = e.i;
             oj = e.j;
             ok = e.k;
-            const double key = gap_key(D.size, oi, oj, ok);
-            stop = !(key < thr) || (radius >= 0.0 && key > radius);
+            stop = !(e.key < thr);
+            if (radius >= 0.0) stop = stop || gap_key(D.size, oi, oj, ok) > radius;
         }
         const unsigned sm = __ballot_sync(FULL, stop);
         const int nval = sm ? __ffs(sm) - 1 : 32;
@@ -590,6 +603,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         for (int i = lane; i < C.np; i += 32) S.fdeg[i] = 0;
         __syncwarp();
         bool fbad = false;
+        bool vbad = false;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             if ((C.lm[k] >> lane) & 1u) {
@@ -610,6 +624,74 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         __syncwarp();
         bool bad = fbad;
         double vpart = 0.0;
+        if constexpr (GUARD) {
+            // FP64 face planes: bisector of the site and point q, n = q,
+            // h = q.q / 2 (vector3.rs:223-239 up to the scale of n); walls
+            // n = +-e_a, h = distance to the wall.
+            const double* blo = P.box_override ? P.box : D.blo;
+            const double* bhi = P.box_override ? P.box + 3 : D.bhi;
+            for (int p = lane; p < C.np; p += 32) {
+                if (S.fdeg[p] == 0) continue;
+                double qx, qy, qz, qh, dist;
+                if (p < 6) {
+                    const int a = p >> 1;
+                    const bool mx = p & 1;
+                    const double s_a = a == 0 ? sx : (a == 1 ? sy : sz);
+                    qh = mx ? (bhi[a] - s_a) : (s_a - blo[a]);
+                    qx = a == 0 ? (mx ? 1.0 : -1.0) : 0.0;
+                    qy = a == 1 ? (mx ? 1.0 : -1.0) : 0.0;
+                    qz = a == 2 ? (mx ? 1.0 : -1.0) : 0.0;
+                    dist = qh;
+                } else {
+                    const uint32_t j = S.psrc[p];
+                    qx = P.spx[j] - sx;
+                    qy = P.spy[j] - sy;
+                    qz = P.spz[j] - sz;
+                    const double q2 = qx * qx + qy * qy + qz * qz;
+                    qh = 0.5 * q2;
+                    dist = 0.5 * sqrt(q2);
+                }
+                S.qx[p] = qx;
+                S.qy[p] = qy;
+                S.qz[p] = qz;
+                S.qh[p] = qh;
+                S.qdist[p] = dist;
+            }
+            __syncwarp();
+            // One Newton step per vertex: residuals of its three planes in
+            // FP64, correction solved in FP32 (Cramer).  A correction larger
+            // than verify_rel * R means the FP32 vertex was not trustworthy:
+            // the cell re-runs in FP64.
+            const float vlim = P.verify_rel * sqrtf((float)R2);
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if ((C.lm[k] >> lane) & 1u) {
+                    const int s = k * 32 + lane;
+                    const uint32_t tt = S.tri[s];
+                    const int a = plane_of(tt, 0), b = plane_of(tt, 1), c = plane_of(tt, 2);
+                    const double x = (double)C.vx[k], y = (double)C.vy[k], z = (double)C.vz[k];
+                    const float ra = (float)(S.qh[a] - (S.qx[a] * x + S.qy[a] * y + S.qz[a] * z));
+                    const float rb = (float)(S.qh[b] - (S.qx[b] * x + S.qy[b] * y + S.qz[b] * z));
+                    const float rc = (float)(S.qh[c] - (S.qx[c] * x + S.qy[c] * y + S.qz[c] * z));
+                    const float ax_ = (float)S.qx[a], ay_ = (float)S.qy[a], az_ = (float)S.qz[a];
+                    const float bx_ = (float)S.qx[b], by_ = (float)S.qy[b], bz_ = (float)S.qz[b];
+                    const float cx_ = (float)S.qx[c], cy_ = (float)S.qy[c], cz_ = (float)S.qz[c];
+                    const float bcx = by_ * cz_ - bz_ * cy_, bcy = bz_ * cx_ - bx_ * cz_, bcz = bx_ * cy_ - by_ * cx_;
+                    const float cax = cy_ * az_ - cz_ * ay_, cay = cz_ * ax_ - cx_ * az_, caz = cx_ * ay_ - cy_ * ax_;
+                    const float abx = ay_ * bz_ - az_ * by_, aby = az_ * bx_ - ax_ * bz_, abz = ax_ * by_ - ay_ * bx_;
+                    const float det = ax_ * bcx + ay_ * bcy + az_ * bcz;
+                    const float inv = 1.0f / det;
+                    const float ddx = (ra * bcx + rb * cax + rc * abx) * inv;
+                    const float ddy = (ra * bcy + rb * cay + rc * aby) * inv;
+                    const float ddz = (ra * bcz + rb * caz + rc * abz) * inv;
+                    if (!(fabsf(ddx) <= vlim && fabsf(ddy) <= vlim && fabsf(ddz) <= vlim)) vbad = true;
+                    S.dx[s] = ddx;
+                    S.dy[s] = ddy;
+                    S.dz[s] = ddz;
+                }
+            }
+            __syncwarp();
+        }
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int p = r * 32 + lane;
@@ -618,37 +700,74 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             if (p < C.np && S.fdeg[p] > 0) {
                 const int start = S.fsta[p];
                 int cur = start, steps = 0;
-                double ax = 0.0, ay = 0.0, az = 0.0;
-                do {
-                    const uint32_t tt = S.tri[cur], aa = S.adj[cur];
-                    const int i = plane_of(tt, 0) == p ? 0 : (plane_of(tt, 1) == p ? 1 : 2);
-                    const int nx = plane_of(aa, i);
-                    if (plane_of(tt, i) != p || nx >= S_t::V) {
-                        bad = true;
-                        break;
-                    }
-                    const double X0 = (double)S.vx[cur], X1 = (double)S.vy[cur], X2 = (double)S.vz[cur];
-                    const double Y0 = (double)S.vx[nx], Y1 = (double)S.vy[nx], Y2 = (double)S.vz[nx];
-                    // the walk runs clockwise seen from outside: Y x X is outward
-                    ax += Y1 * X2 - Y2 * X1;
-                    ay += Y2 * X0 - Y0 * X2;
-                    az += Y0 * X1 - Y1 * X0;
-                    cur = nx;
-                    ++steps;
-                } while (cur != start && steps <= S_t::V);
+                if constexpr (GUARD) {
+                    // Fan from the first vertex (weighted_normal,
+                    // polyhedron.rs:776-808) on refined positions:
+                    // (x - anchor) = (x32 - a32) + (dx - da), in FP32.
+                    const float a0 = (float)S.vx[start], a1 = (float)S.vy[start], a2 = (float)S.vz[start];
+                    const float e0 = S.dx[start], e1 = S.dy[start], e2 = S.dz[start];
+                    float ux = 0.f, uy = 0.f, uz = 0.f, wx = 0.f, wy = 0.f, wz = 0.f;
+                    do {
+                        const uint32_t tt = S.tri[cur], aa = S.adj[cur];
+                        const int i = plane_of(tt, 0) == p ? 0 : (plane_of(tt, 1) == p ? 1 : 2);
+                        const int nx = plane_of(aa, i);
+                        if (plane_of(tt, i) != p || nx >= S_t::V) {
+                            bad = true;
+                            break;
+                        }
+                        const float vx_ = ((float)S.vx[nx] - a0) + (S.dx[nx] - e0);
+                        const float vy_ = ((float)S.vy[nx] - a1) + (S.dy[nx] - e1);
+                        const float vz_ = ((float)S.vz[nx] - a2) + (S.dz[nx] - e2);
+                        if (steps > 0) {
+                            wx += uy * vz_ - uz * vy_;
+                            wy += uz * vx_ - ux * vz_;
+                            wz += ux * vy_ - uy * vx_;
+                        }
+                        ux = vx_;
+                        uy = vy_;
+                        uz = vz_;
+                        cur = nx;
+                        ++steps;
+                    } while (cur != start && steps <= S_t::V);
+                    const double area = 0.5 * sqrt((double)wx * wx + (double)wy * wy + (double)wz * wz);
+                    farea[r] = area;
+                    vpart += area * S.qdist[p];
+                } else {
+                    double ax = 0.0, ay = 0.0, az = 0.0;
+                    do {
+                        const uint32_t tt = S.tri[cur], aa = S.adj[cur];
+                        const int i = plane_of(tt, 0) == p ? 0 : (plane_of(tt, 1) == p ? 1 : 2);
+                        const int nx = plane_of(aa, i);
+                        if (plane_of(tt, i) != p || nx >= S_t::V) {
+                            bad = true;
+                            break;
+                        }
+                        const double X0 = (double)S.vx[cur], X1 = (double)S.vy[cur], X2 = (double)S.vz[cur];
+                        const double Y0 = (double)S.vx[nx], Y1 = (double)S.vy[nx], Y2 = (double)S.vz[nx];
+                        // the walk runs clockwise seen from outside: Y x X is outward
+                        ax += Y1 * X2 - Y2 * X1;
+                        ay += Y2 * X0 - Y0 * X2;
+                        az += Y0 * X1 - Y1 * X0;
+                        cur = nx;
+                        ++steps;
+                    } while (cur != start && steps <= S_t::V);
+                    const double A0 = (double)S.vx[start], A1 = (double)S.vy[start], A2 = (double)S.vz[start];
+                    vpart += (ax * A0 + ay * A1 + az * A2) * 0.5;
+                    farea[r] = 0.5 * sqrt(ax * ax + ay * ay + az * az);
+                }
                 bad |= (cur != start) || (steps != (int)S.fdeg[p]) || steps < 3;
-                const double A0 = (double)S.vx[start], A1 = (double)S.vy[start], A2 = (double)S.vz[start];
-                vpart += ax * A0 + ay * A1 + az * A2;
-                farea[r] = 0.5 * sqrt(ax * ax + ay * ay + az * az);
                 fdegr[r] = steps;
             }
         }
-        vol = warp_sum_d(vpart) / 6.0;
+        // volume: sum of pyramids from the site, area * height / 3
+        // (compute_volume, polyhedron.rs:838-855)
+        vol = warp_sum_d(vpart) / 3.0;
 #pragma unroll
         for (int r = 0; r < R; ++r) F += __popc(__ballot_sync(FULL, fdegr[r] > 0));
         // Every vertex has three faces: V - E + F = 2 with E = 3V/2.
         if (nlive > 0 && F != nlive / 2 + 2) bad = true;
         if (__any_sync(FULL, bad)) status = ST_DEGEN;
+        else if (GUARD && __any_sync(FULL, vbad)) status = ST_VERIFY;
     }
 
     // ---- outputs ----
@@ -660,7 +779,8 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         if (lane == 0) {
             uint32_t* list = nullptr;
             unsigned* count = nullptr;
-            if (status == ST_GUARD || status == ST_DEGEN) {
+            if (P.reasons) atomicAdd(&P.reasons[status & 7], 1u);
+            if (status == ST_GUARD || status == ST_DEGEN || status == ST_VERIFY) {
                 list = P.list_fp64;
                 count = P.list_fp64_count;
             } else if (status == ST_VCAP || status == ST_PCAP) {
@@ -711,9 +831,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 for (int kk = 0; kk < K; ++kk)
                     if (kk < k) vi += __popc(C.lm[kk]);
                 const int s = k * 32 + lane;
-                G->verts[3 * vi] = (double)S.vx[s];
-                G->verts[3 * vi + 1] = (double)S.vy[s];
-                G->verts[3 * vi + 2] = (double)S.vz[s];
+                G->verts[3 * vi] = (double)S.vx[s] + (GUARD ? (double)S.dx[s % S_t::VF] : 0.0);
+                G->verts[3 * vi + 1] = (double)S.vy[s] + (GUARD ? (double)S.dy[s % S_t::VF] : 0.0);
+                G->verts[3 * vi + 2] = (double)S.vz[s] + (GUARD ? (double)S.dz[s % S_t::VF] : 0.0);
             }
         }
 #pragma unroll
@@ -796,31 +916,37 @@ __global__ void k_clip(ClipParams P) {
     }
 }
 
+// Raise the kernel's dynamic shared memory limit to what `bytes` needs (once
+// per size); kept out of stream capture by the host's warm-up calls.
+template <typename T, int K, bool GEO>
+cudaError_t configure_smem(size_t bytes) {
+    static size_t configured = 0;
+    if (bytes <= configured) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_clip<T, K, GEO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) configured = bytes;
+    return e;
+}
+
 template <typename T, int K, bool GEO>
 cudaError_t launch_t(const ClipParams& p, int wpb, int blocks, cudaStream_t s) {
     const size_t sm = sizeof(Smem<T, K>) * (size_t)wpb;
-    auto fn = k_clip<T, K, GEO>;
-    static size_t configured = 0;   // attribute calls stay out of stream capture once set
-    if (sm > configured) {
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-        if (e != cudaSuccess) return e;
-        configured = 100 * 1024;
-    }
-    fn<<<blocks, 32 * wpb, sm, s>>>(p);
+    cudaError_t e = configure_smem<T, K, GEO>(sm);
+    if (e != cudaSuccess) return e;
+    k_clip<T, K, GEO><<<blocks, 32 * wpb, sm, s>>>(p);
     return cudaGetLastError();
 }
 
 template <typename T, int K, bool GEO>
 int blocks_t(int wpb, int device) {
     const size_t sm = sizeof(Smem<T, K>) * (size_t)wpb;
-    auto fn = k_clip<T, K, GEO>;
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 32 * wpb, sm);
-    int nsm = 0;
+    int per = 0, nsm = 0;
+    if (configure_smem<T, K, GEO>(sm) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_clip<T, K, GEO>, 32 * wpb, sm) != cudaSuccess)
+        per = 1;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    cudaGetLastError();   // leave no sticky error behind a failed query
     if (per < 1) per = 1;
-    return per * nsm;
+    return per * (nsm > 0 ? nsm : 1);
 }
 
 }  // namespace clipk

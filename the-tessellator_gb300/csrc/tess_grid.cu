@@ -85,14 +85,18 @@ __global__ void k_grid_params(GridBuffers g) {
     if (cheb > D.cpd - 1) cheb = D.cpd - 1;
     if (cheb < 0) cheb = 0;
     D.cheb = cheb;
+    // The table holds every offset of the grid when that fits; otherwise the
+    // offsets with key <= kmax, and the walk continues ring by ring.
+    const bool complete = cheb == D.cpd - 1 && (2 * cheb + 1) * (2 * cheb + 1) * (2 * cheb + 1) <= kMaxTable;
     if (m == DBL_MAX) {          // every point identical: only the own bin holds points
         D.min_size = 0.0;
         D.tab_kmax = INFINITY;
+        D.cheb = 0;
     } else {
         D.min_size = m;
         const int gaps = cheb - 1;
-        D.tab_kmax = (cheb >= D.cpd - 1) ? (double)INFINITY
-                                         : __dmul_rn(__dmul_rn((double)gaps, m), __dmul_rn((double)gaps, m));
+        D.tab_kmax = complete ? (double)INFINITY
+                              : __dmul_rn(__dmul_rn((double)gaps, m), __dmul_rn((double)gaps, m));
     }
 }
 

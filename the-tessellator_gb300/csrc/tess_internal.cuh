@@ -30,6 +30,7 @@ enum CellStatus : uint8_t {
     ST_PCAP = 3,        // face (plane) capacity exceeded -> larger capacity re-run
     ST_DEGEN = 4,       // inconsistent topology (degenerate input) -> FP64 re-run / error
     ST_POOL = 5,        // face pool full -> host grows the pool
+    ST_VERIFY = 6,      // FP32 vertex failed the FP64 check -> FP64 re-run
     ST_PENDING = 255    // not computed yet
 };
 
@@ -170,6 +171,7 @@ struct ClipParams {
     uint32_t* list_cap;           // capacity overflow cells or null
     unsigned int* list_cap_count;
     unsigned int* fail_count;     // cells left with an error status
+    unsigned int* reasons;        // per status code: cells routed or failed for it
     // options
     double search_radius;         // < 0: none
     int64_t target_group;         // < 0: none

@@ -44,7 +44,8 @@ class Stats(C.Structure):
     _fields_ = [("cells", C.c_uint64), ("faces", C.c_uint64), ("rerun_fp64", C.c_uint64),
                 ("rerun_capacity", C.c_uint64), ("failed", C.c_uint64),
                 ("table_entries", C.c_uint64), ("ms_grid", C.c_double), ("ms_clip", C.c_double),
-                ("ms_rerun", C.c_double), ("ms_csr", C.c_double), ("launches", C.c_uint64)]
+                ("ms_rerun", C.c_double), ("ms_csr", C.c_double), ("launches", C.c_uint64),
+                ("rerun_guard", C.c_uint64), ("rerun_verify", C.c_uint64), ("rerun_degenerate", C.c_uint64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
