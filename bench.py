@@ -319,7 +319,8 @@ def run_ours(args, ws, rank, local):
         "passes_ms": {"grid": float(np.mean(grid_ms)), "clip_first_pass": float(np.mean(clip_ms)),
                       "reruns": float(np.mean(rerun_ms)), "csr": float(np.mean(csr_ms))},
         "reruns": {"fp64": int(st1["rerun_fp64"]), "capacity": int(st1["rerun_capacity"]),
-                   "failed": int(st1["failed"])},
+                   "failed": int(st1["failed"]), "guard": int(st1["rerun_guard"]),
+                   "verify": int(st1["rerun_verify"]), "degenerate": int(st1["rerun_degenerate"])},
     }
     if rank == 0 and not args.no_cpu_baseline:
         rate, ost, sample_cells, sample_desc = cpu_baseline(pts, batched, args.cpu_seconds)

@@ -141,7 +141,7 @@ def test_batch_matches_single_diagrams(tess, oracle_mod):
             rv, ro, ri, ra, _, _ = r.compute_all()
             tol = 1e-12 if prec == "fp64" else 1e-6
             assert np.max(np.abs(vol[s:e] - rv) / rv) <= tol
-            assert math.isclose(vol[s:e].sum(), float(np.prod(boxes[dgi, 3:])), rel_tol=1e-9)
+            assert math.isclose(vol[s:e].sum(), float(np.prod(boxes[dgi, 3:])), rel_tol=tol * 10)
             got = nbr[int(coffs[s]):int(coffs[e])].astype(np.int64)
             assert np.array_equal(got, ri)
         # a second launch replays the captured graph with the same results

@@ -105,10 +105,10 @@ def test_oblong_and_offset_boxes(tess, oracle_mod):
 def test_default_bounding_box(tess, oracle_mod):
     """No container: the Diagram bounding box, grown from the origin."""
     rng = np.random.default_rng(8)
-    pts = 2.0 + rng.random((800, 3))   # the box becomes [0, 3]^3
+    pts = 2.0 + rng.random((800, 3))   # the box becomes [0, max]^3, max < 3
     gpu, _ = gpu_all(tess, pts, "fp64")
     ref = ref_all(oracle_mod, pts)
-    compare("fp64", gpu, ref, len(pts), check_sum=27.0)
+    compare("fp64", gpu, ref, len(pts), check_sum=float(np.prod(pts.max(axis=0))))
 
 
 @pytest.mark.parametrize("n", [1, 2, 5])

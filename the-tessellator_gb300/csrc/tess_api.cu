@@ -98,6 +98,8 @@ struct Engine {
     double* d_spx = nullptr;
     double* d_spy = nullptr;
     double* d_spz = nullptr;
+    float* d_shi = nullptr;
+    float* d_slo = nullptr;
     uint32_t* d_sgroup = nullptr;
     TabEntry* d_table = nullptr;
     int* d_err = nullptr;
@@ -140,7 +142,7 @@ struct Engine {
         graph = nullptr;
         dfree(d_xyz); dfree(d_groups); dfree(d_desc); dfree(d_chunk_diag); dfree(d_chunk_start);
         dfree(d_bounds); dfree(d_bin); dfree(d_rank); dfree(d_delims); dfree(d_scan_tmp);
-        dfree(d_sorted); dfree(d_inv); dfree(d_spx); dfree(d_spy); dfree(d_spz); dfree(d_sgroup);
+        dfree(d_sorted); dfree(d_inv); dfree(d_spx); dfree(d_spy); dfree(d_spz); dfree(d_shi); dfree(d_slo); dfree(d_sgroup);
         dfree(d_table); dfree(d_err); dfree(d_vol); dfree(d_nface); dfree(d_fstart); dfree(d_status);
         dfree(d_fnbr); dfree(d_farea); dfree(d_fcursor);
         for (auto& l : d_list) dfree(l);
@@ -267,6 +269,8 @@ tess_status engine_init(Engine& E, const tess_config* cfg, std::vector<DiagDesc>
     TRY(dalloc(&E.d_spx, n));
     TRY(dalloc(&E.d_spy, n));
     TRY(dalloc(&E.d_spz, n));
+    TRY(dalloc(&E.d_shi, 3 * n));
+    TRY(dalloc(&E.d_slo, 3 * n));
     TRY(dalloc(&E.d_table, E.table_total));
     TRY(dalloc(&E.d_err, 1));
     TRY(dalloc(&E.d_vol, n));
@@ -307,6 +311,8 @@ GridBuffers grid_buffers(Engine& E) {
     g.spx = E.d_spx;
     g.spy = E.d_spy;
     g.spz = E.d_spz;
+    g.shi = E.d_shi;
+    g.slo = E.d_slo;
     g.sgroup = E.d_sgroup;
     g.table = E.d_table;
     g.table_gaps = E.cfg.table_gaps;
@@ -354,6 +360,8 @@ ClipParams base_params(Engine& E) {
     p.spx = E.d_spx;
     p.spy = E.d_spy;
     p.spz = E.d_spz;
+    p.shi = E.d_shi;
+    p.slo = E.d_slo;
     p.sorted = E.d_sorted;
     p.delims = E.d_delims;
     p.sgroup = E.d_sgroup;

@@ -63,6 +63,7 @@ struct Smem {
     uint32_t adj[V];                  // neighbours n0 | n1 << 8 | n2 << 16
     uint32_t fdeg[P];                 // finalize: live vertices per face
     uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
+    uint16_t item[32];                // boundary edges of a cut: slot | edge << 8
     int32_t flist[P];                 // finalize: compacted face ids
     uint8_t fsta[P];                  // finalize: one vertex of each face
     uint8_t mapf[P], maps[P];         // new-vertex ring maps
@@ -71,7 +72,8 @@ struct Smem {
     // from the site, and per-vertex FP32 corrections to the FP64 position.
     static constexpr int PF = sizeof(T) == 4 ? P : 1;
     static constexpr int VF = sizeof(T) == 4 ? V : 1;
-    double qx[PF], qy[PF], qz[PF], qh[PF], qdist[PF];
+    double qx[PF], qy[PF], qz[PF], qh[PF];
+    float fqx[PF], fqy[PF], fqz[PF], qdist[PF];
     float dx[VF], dy[VF], dz[VF];
 };
 
@@ -180,8 +182,8 @@ struct CellRegs {
 // Clip the cell by {x : n.x - off <= 0}.  Returns 1 when vertices were cut
 // off, 0 when nothing was Outside, or -status.
 template <typename T, int K, bool GUARD>
-__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, int32_t id, uint32_t src,
-                   T guard, int lane) {
+__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, const uint32_t* sorted,
+                   uint32_t pt_base, uint32_t src, T guard, int lane) {
     using S_t = Smem<T, K>;
     T sd[K];
     uint32_t om[K];
@@ -256,6 +258,96 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, in
     }
     if (K == 8) fm[K - 1] &= 0x7FFFFFFFu;
     if (nlive + B > S_t::VUSE) return -ST_VCAP;
+    const int f = C.np;
+    if (B <= 32) {
+        // One boundary edge per lane.  Owners list their edges at their
+        // prefix positions; every lane then reads its edge's data before any
+        // freed slot is reused.
+        {
+            int qq = q;
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+#pragma unroll
+                for (int e = 0; e < 3; ++e)
+                    if (bnd & (1u << (3 * k + e))) S.item[qq++] = (uint16_t)((k * 32 + lane) | (e << 8));
+        }
+        __syncwarp();
+        const bool act = lane < B;
+        int y = 0, a = 0, b = 0, slot = 0;
+        uint32_t ty = 0;
+        T px = 0, py = 0, pz = 0;
+        if (act) {
+            const uint32_t it = S.item[lane];
+            const int x = it & 0xFF, e = it >> 8;
+            const uint32_t xt_ = S.tri[x], xa_ = S.adj[x];
+            a = plane_of(xt_, e);
+            b = plane_of(xt_, e == 2 ? 0 : e + 1);
+            y = plane_of(xa_, e);
+            const T xx = S.vx[x], xy = S.vy[x], xz = S.vz[x], xsd = S.vsd[x];
+            const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
+            ty = S.tri[y];
+            // intersection(outside X, inside Y) (vector3.rs:213-219); an
+            // Incident Y is kept as the new vertex (polyhedron.rs:554-565)
+            const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / (xsd - ysd);
+            px = xx + (yx - xx) * t;
+            py = xy + (yy - xy) * t;
+            pz = xz + (yz - xz) * t;
+            slot = select_k<K>(fm, lane);
+        }
+        __syncwarp();
+        if (act) {
+            S.vx[slot] = px;
+            S.vy[slot] = py;
+            S.vz[slot] = pz;
+            S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
+            // Y's pointer back to X is the edge (b, a) of Y's triple.
+            const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
+                           : (plane_of(ty, 1) == b && plane_of(ty, 2) == a) ? 1
+                                                                            : 2;
+            reinterpret_cast<uint8_t*>(S.adj)[4 * y + yi] = (uint8_t)slot;
+            S.mapf[a] = (uint8_t)slot;
+            S.maps[b] = (uint8_t)slot;
+        }
+        __syncwarp();
+        bool bad = false;
+        if (act) {
+            const int n1 = S.mapf[b], n2 = S.maps[a];
+            bad = (S.mapf[a] != slot) || (S.maps[b] != slot) || n1 == 0xFF || n2 == 0xFF;
+            S.adj[slot] = (uint32_t)y | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
+        }
+        __syncwarp();
+        if (act) {
+            S.mapf[a] = 0xFF;
+            S.maps[b] = 0xFF;
+        }
+        if (__any_sync(FULL, bad)) return -ST_DEGEN;
+        uint32_t newm[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            newm[k] = __reduce_or_sync(FULL, (act && (slot >> 5) == k) ? (1u << (slot & 31)) : 0u);
+            C.lm[k] = (C.lm[k] & ~om[k]) | newm[k];
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if ((newm[k] >> lane) & 1u) {
+                const int s = k * 32 + lane;
+                C.vx[k] = S.vx[s];
+                C.vy[k] = S.vy[s];
+                C.vz[k] = S.vz[s];
+            }
+        }
+        if (lane == 0) {
+            S.px[f] = nx;
+            S.py[f] = ny;
+            S.pz[f] = nz;
+            S.pd[f] = off;
+            S.pid[f] = (int32_t)(sorted[src] - pt_base);
+            S.psrc[f] = src;
+        }
+        C.np = f + 1;
+        __syncwarp();
+        return 1;
+    }
     __syncwarp();
 
     // Pass 1: place the new vertices.
@@ -263,7 +355,6 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, in
 #pragma unroll
     for (int k = 0; k < K; ++k) newm[k] = 0;
     int nslot[3 * K], na[3 * K], nbp[3 * K], ny_[3 * K];
-    const int f = C.np;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
 #pragma unroll
@@ -276,7 +367,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, in
                 const int y = plane_of(xa[k], e);
                 const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
                 const T xsd = sd[k];
-                const T t = xsd / (xsd - ysd);
+                const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / (xsd - ysd);
                 const T px = C.vx[k] + (yx - C.vx[k]) * t;
                 const T py = C.vy[k] + (yy - C.vy[k]) * t;
                 const T pz = C.vz[k] + (yz - C.vz[k]) * t;
@@ -343,7 +434,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, in
         S.py[f] = ny;
         S.pz[f] = nz;
         S.pd[f] = off;
-        S.pid[f] = id;
+        S.pid[f] = (int32_t)(sorted[src] - pt_base);
         S.psrc[f] = src;
     }
     C.np = f + 1;
@@ -411,6 +502,19 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         sz = P.spz[gs];
         self = gs;
         orig = P.sorted[gs];
+    }
+    // FP32 form: the site as an FP32 pair (hi + lo), so candidate offsets
+    // (p - site) come out of FP32 arithmetic with FP64-rounded accuracy.
+    float shx = 0.f, shy = 0.f, shz = 0.f, slx = 0.f, sly = 0.f, slz = 0.f;
+    if constexpr (GUARD) {
+        if (P.at_point) {
+            shx = __double2float_rn(sx); slx = __double2float_rn(sx - (double)shx);
+            shy = __double2float_rn(sy); sly = __double2float_rn(sy - (double)shy);
+            shz = __double2float_rn(sz); slz = __double2float_rn(sz - (double)shz);
+        } else {
+            shx = P.shi[3ull * gs]; shy = P.shi[3ull * gs + 1]; shz = P.shi[3ull * gs + 2];
+            slx = P.slo[3ull * gs]; sly = P.slo[3ull * gs + 1]; slz = P.slo[3ull * gs + 2];
+        }
     }
 
     // ---- the container box, translated by -site (polyhedron.rs:268-392) ----
@@ -496,27 +600,59 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     else hi = mid - 1;
                 }
                 j = S.cbeg[lo] + (c - S.cpref[lo]);
-                rx = (T)(P.spx[j] - sx);
-                ry = (T)(P.spy[j] - sy);
-                rz = (T)(P.spz[j] - sz);
+                if constexpr (GUARD) {
+                    rx = (T)((P.shi[3ull * j] - shx) + (P.slo[3ull * j] - slx));
+                    ry = (T)((P.shi[3ull * j + 1] - shy) + (P.slo[3ull * j + 1] - sly));
+                    rz = (T)((P.shi[3ull * j + 2] - shz) + (P.slo[3ull * j + 2] - slz));
+                } else {
+                    rx = (T)(P.spx[j] - sx);
+                    ry = (T)(P.spy[j] - sy);
+                    rz = (T)(P.spz[j] - sz);
+                }
                 r2 = rx * rx + ry * ry + rz * rz;
                 keep = (j != self) && r2 > (T)0 && r2 < lim;
                 if (keep && tgroup >= 0) keep = (int64_t)(P.sgroup ? P.sgroup[j] : 0u) == tgroup;
             }
-            unsigned km = __ballot_sync(FULL, keep);
-            while (km) {
-                const int src = __ffs(km) - 1;
-                km &= km - 1;
+            const int nkeep = __popc(__ballot_sync(FULL, keep));
+            if (nkeep == 0) continue;
+            // Nearest first: a bitonic sort of the window by distance (ties by
+            // lane) lets the closest bisectors shrink the cell before the
+            // farther ones are tested.
+            int order = lane;
+            if (nkeep > 1) {
+                float key = keep ? (float)r2 : INFINITY;
+#pragma unroll
+                for (int k2 = 2; k2 <= 32; k2 <<= 1) {
+#pragma unroll
+                    for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
+                        const float ok = __shfl_xor_sync(FULL, key, j2);
+                        const int oi = __shfl_xor_sync(FULL, order, j2);
+                        const bool asc = (lane & k2) == 0;
+                        const bool lower = (lane & j2) == 0;
+                        const bool other_less = ok < key || (ok == key && oi < order);
+                        if (other_less == (lower == asc)) {
+                            key = ok;
+                            order = oi;
+                        }
+                    }
+                }
+            } else {
+                order = __ffs(__ballot_sync(FULL, keep)) - 1;
+            }
+            for (int q = 0; q < nkeep; ++q) {
+                const int src = __shfl_sync(FULL, order, q);
                 const T cx = __shfl_sync(FULL, rx, src);
                 const T cy = __shfl_sync(FULL, ry, src);
                 const T cz = __shfl_sync(FULL, rz, src);
                 const T c2 = __shfl_sync(FULL, r2, src);
                 const uint32_t cj = __shfl_sync(FULL, j, src);
-                if (!(c2 < (T)4 * R2 * (T)kStopMargin)) continue;
+                if (!(c2 < (T)4 * R2 * (T)kStopMargin)) {
+                    if (GUARD) break;   // sorted: every later candidate is as far
+                    continue;
+                }
                 T nx, ny, nz, off;
                 bisector(cx, cy, cz, c2, nx, ny, nz, off);
-                const int32_t id = (int32_t)(P.sorted[cj] - D.pt_base);
-                const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, id, cj, guard, lane);
+                const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, P.sorted, D.pt_base, cj, guard, lane);
                 if (r < 0) return -r;
                 if (r > 0) {
                     R2 = live_r2(C, lane);
@@ -632,7 +768,8 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             const double* bhi = P.box_override ? P.box + 3 : D.bhi;
             for (int p = lane; p < C.np; p += 32) {
                 if (S.fdeg[p] == 0) continue;
-                double qx, qy, qz, qh, dist;
+                double qx, qy, qz, qh;
+                float dist;
                 if (p < 6) {
                     const int a = p >> 1;
                     const bool mx = p & 1;
@@ -641,7 +778,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     qx = a == 0 ? (mx ? 1.0 : -1.0) : 0.0;
                     qy = a == 1 ? (mx ? 1.0 : -1.0) : 0.0;
                     qz = a == 2 ? (mx ? 1.0 : -1.0) : 0.0;
-                    dist = qh;
+                    dist = (float)qh;
                 } else {
                     const uint32_t j = S.psrc[p];
                     qx = P.spx[j] - sx;
@@ -649,12 +786,15 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     qz = P.spz[j] - sz;
                     const double q2 = qx * qx + qy * qy + qz * qz;
                     qh = 0.5 * q2;
-                    dist = 0.5 * sqrt(q2);
+                    dist = 0.5f * sqrtf((float)q2);
                 }
                 S.qx[p] = qx;
                 S.qy[p] = qy;
                 S.qz[p] = qz;
                 S.qh[p] = qh;
+                S.fqx[p] = (float)qx;
+                S.fqy[p] = (float)qy;
+                S.fqz[p] = (float)qz;
                 S.qdist[p] = dist;
             }
             __syncwarp();
@@ -673,9 +813,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     const float ra = (float)(S.qh[a] - (S.qx[a] * x + S.qy[a] * y + S.qz[a] * z));
                     const float rb = (float)(S.qh[b] - (S.qx[b] * x + S.qy[b] * y + S.qz[b] * z));
                     const float rc = (float)(S.qh[c] - (S.qx[c] * x + S.qy[c] * y + S.qz[c] * z));
-                    const float ax_ = (float)S.qx[a], ay_ = (float)S.qy[a], az_ = (float)S.qz[a];
-                    const float bx_ = (float)S.qx[b], by_ = (float)S.qy[b], bz_ = (float)S.qz[b];
-                    const float cx_ = (float)S.qx[c], cy_ = (float)S.qy[c], cz_ = (float)S.qz[c];
+                    const float ax_ = S.fqx[a], ay_ = S.fqy[a], az_ = S.fqz[a];
+                    const float bx_ = S.fqx[b], by_ = S.fqy[b], bz_ = S.fqz[b];
+                    const float cx_ = S.fqx[c], cy_ = S.fqy[c], cz_ = S.fqz[c];
                     const float bcx = by_ * cz_ - bz_ * cy_, bcy = bz_ * cx_ - bx_ * cz_, bcz = bx_ * cy_ - by_ * cx_;
                     const float cax = cy_ * az_ - cz_ * ay_, cay = cz_ * ax_ - cx_ * az_, caz = cx_ * ay_ - cy_ * ax_;
                     const float abx = ay_ * bz_ - az_ * by_, aby = az_ * bx_ - ax_ * bz_, abz = ax_ * by_ - ay_ * bx_;
@@ -729,9 +869,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                         cur = nx;
                         ++steps;
                     } while (cur != start && steps <= S_t::V);
-                    const double area = 0.5 * sqrt((double)wx * wx + (double)wy * wy + (double)wz * wz);
-                    farea[r] = area;
-                    vpart += area * S.qdist[p];
+                    const float area = 0.5f * sqrtf(wx * wx + wy * wy + wz * wz);
+                    farea[r] = (double)area;
+                    vpart += (double)(area * S.qdist[p]);
                 } else {
                     double ax = 0.0, ay = 0.0, az = 0.0;
                     do {

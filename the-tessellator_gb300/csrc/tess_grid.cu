@@ -222,9 +222,17 @@ __global__ void k_gather(GridBuffers g) {
     if (s >= g.total) return;
     const uint32_t i = g.sorted[s];
     g.inv[i] = s;
-    g.spx[s] = g.xyz[3ull * i];
-    g.spy[s] = g.xyz[3ull * i + 1];
-    g.spz[s] = g.xyz[3ull * i + 2];
+    const double x = g.xyz[3ull * i], y = g.xyz[3ull * i + 1], z = g.xyz[3ull * i + 2];
+    g.spx[s] = x;
+    g.spy[s] = y;
+    g.spz[s] = z;
+    const float hx = __double2float_rn(x), hy = __double2float_rn(y), hz = __double2float_rn(z);
+    g.shi[3ull * s] = hx;
+    g.shi[3ull * s + 1] = hy;
+    g.shi[3ull * s + 2] = hz;
+    g.slo[3ull * s] = __double2float_rn(x - (double)hx);
+    g.slo[3ull * s + 1] = __double2float_rn(y - (double)hy);
+    g.slo[3ull * s + 2] = __double2float_rn(z - (double)hz);
     if (g.sgroup) g.sgroup[s] = g.groups[i];
 }
 

@@ -128,6 +128,8 @@ struct GridBuffers {
     double* spx;
     double* spy;
     double* spz;
+    float* shi;                 // FP32 split of the sorted positions:
+    float* slo;                 // x = shi + slo, 3 floats per point each (AoS)
     uint32_t* sgroup;           // null when groups is null
     TabEntry* table;
     int table_gaps;
@@ -147,6 +149,8 @@ struct ClipParams {
     const double* spx;
     const double* spy;
     const double* spz;
+    const float* shi;               // x = shi + slo (FP32 pair), AoS
+    const float* slo;
     const uint32_t* sorted;
     const uint32_t* delims;
     const uint32_t* sgroup;
