@@ -59,10 +59,12 @@ typedef enum {
 #define TESS_FLAG_TIMING 1u   /* record per-pass device times (tess_stats) */
 
 typedef struct {
-    /* Guard band of the FP32 form, relative to the current cell radius. */
+    /* FP32 form, guard band: a plane test of vertex v is undecided (the cell
+     * re-runs in FP64) when |signed distance| <= e_v + guard_rel * R, with
+     * e_v the vertex's tracked error bound and R the cell radius. */
     double guard_rel;
-    /* Largest allowed |FP32 vertex - FP64 vertex| / cell radius before a
-     * cell is re-run in FP64. */
+    /* FP32 form, final check: the FP64 correction of every vertex must stay
+     * within 2 e_v + verify_rel * R, else the cell re-runs in FP64. */
     double verify_rel;
     /* Points per bin; the reference's cell_density() is 1.25 (celery.rs:185-188). */
     double bin_density;

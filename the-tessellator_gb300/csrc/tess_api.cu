@@ -170,8 +170,8 @@ struct Engine {
 };
 
 void fill_defaults(tess_config* c) {
-    c->guard_rel = 2e-5;
-    c->verify_rel = 1e-5;
+    c->guard_rel = 1e-6;
+    c->verify_rel = 1e-6;
     c->bin_density = 1.25;
     c->table_gaps = 8;
     c->warps_per_block = 8;

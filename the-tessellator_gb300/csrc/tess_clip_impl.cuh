@@ -63,7 +63,7 @@ struct Smem {
     uint32_t adj[V];                  // neighbours n0 | n1 << 8 | n2 << 16
     uint32_t fdeg[P];                 // finalize: live vertices per face
     uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
-    uint16_t item[32];                // boundary edges of a cut: slot | edge << 8
+    uint16_t items[V + 32];           // boundary edges of a cut: slot | edge << 8
     int32_t flist[P];                 // finalize: compacted face ids
     uint8_t fsta[P];                  // finalize: one vertex of each face
     uint8_t mapf[P], maps[P];         // new-vertex ring maps
@@ -75,6 +75,7 @@ struct Smem {
     double qx[PF], qy[PF], qz[PF], qh[PF];
     float fqx[PF], fqy[PF], fqz[PF], qdist[PF];
     float dx[VF], dy[VF], dz[VF];
+    float ve[VF];                     // vertex error bounds (mirror of CellRegs::ve)
 };
 
 __device__ __forceinline__ unsigned warp_incl_scan_u(unsigned v, int lane) {
@@ -152,16 +153,18 @@ __device__ __forceinline__ double sdist(double nx, double ny, double nz, double 
 }
 
 // Bisector of the site (origin) and r (halfway_from_origin_to, vector3.rs:223-239).
+// FP32 form: the same plane unnormalised, n = r, off = r.r / 2; rn = |r|.
 __device__ __forceinline__ void bisector(float rx, float ry, float rz, float r2, float& nx, float& ny,
-                                         float& nz, float& off) {
-    const float inv = rsqrtf(r2);
-    nx = rx * inv;
-    ny = ry * inv;
-    nz = rz * inv;
-    off = 0.5f * r2 * inv;
+                                         float& nz, float& off, float& rn) {
+    nx = rx;
+    ny = ry;
+    nz = rz;
+    off = 0.5f * r2;
+    rn = sqrtf(r2);
 }
 __device__ __forceinline__ void bisector(double rx, double ry, double rz, double r2, double& nx,
-                                         double& ny, double& nz, double& off) {
+                                         double& ny, double& nz, double& off, double& rn) {
+    rn = 1.0;
     const double inv = 1.0 / sqrt(r2);
     nx = rx * inv;
     ny = ry * inv;
@@ -175,15 +178,24 @@ __device__ __forceinline__ float round_up_f(double x) { return __double2float_ru
 template <typename T, int K>
 struct CellRegs {
     T vx[K], vy[K], vz[K];
+    T ve[K];          // FP32 form: bound on each vertex's position error
     uint32_t lm[K];   // live masks (warp-uniform)
     int np;           // planes used (warp-uniform)
 };
 
-// Clip the cell by {x : n.x - off <= 0}.  Returns 1 when vertices were cut
-// off, 0 when nothing was Outside, or -status.
+// Clip the cell by the half-space {x : n.x - off <= 0}.
+//   FP64 form: n is the unit normal of the bisector and off its offset; a
+//     vertex is Outside when n.v - off > 1e-12 (vector3.rs:170-193,
+//     polyhedron.rs:221).
+//   FP32 form: n = r and off = r.r / 2 (the same plane, scaled by rn = |r|).
+//     Every vertex carries a bound e_v on its position error.  A test with
+//     |n.v - off| <= rn * (e_v + cR), cR bounding the plane's own rounding,
+//     cannot be decided in FP32: the cell goes to the FP64 form (ST_GUARD).
+// Returns 1 when vertices were cut off, 0 when nothing was Outside, or
+// -status.
 template <typename T, int K, bool GUARD>
-__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, const uint32_t* sorted,
-                   uint32_t pt_base, uint32_t src, T guard, int lane) {
+__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T rn, T cR,
+                   const uint32_t* sorted, uint32_t pt_base, uint32_t src, int lane) {
     using S_t = Smem<T, K>;
     T sd[K];
     uint32_t om[K];
@@ -192,8 +204,8 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, co
     for (int k = 0; k < K; ++k) {
         const bool live = (C.lm[k] >> lane) & 1u;
         sd[k] = sdist(nx, ny, nz, off, C.vx[k], C.vy[k], C.vz[k]);
-        const bool out = live && sd[k] > (T)kTolerance;
-        if (GUARD) gh |= live && fabs(sd[k]) < guard;
+        const bool out = live && sd[k] > (GUARD ? (T)0 : (T)kTolerance);
+        if constexpr (GUARD) gh |= live && fabs(sd[k]) <= rn * (C.ve[k] + cR);
         om[k] = __ballot_sync(FULL, out);
     }
     if (GUARD && __any_sync(FULL, gh)) return -ST_GUARD;
@@ -203,9 +215,9 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, co
     if (!anyo) return 0;
     if (C.np >= S_t::P) return -ST_PCAP;
 
-    // Signed distances of live vertices, read by the lanes owning Outside
-    // neighbours; triples/neighbours of my Outside vertices, read before any
-    // slot is reused.
+    // Signed distances of live vertices go to shared memory for the lanes
+    // that place new vertices; my Outside vertices' triples and neighbours are
+    // read before any slot is reused.
     uint32_t xt[K], xa[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -230,6 +242,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, co
         }
     }
     if (__any_sync(FULL, badref)) return -ST_DEGEN;
+    // Boundary edges: edges of Outside vertices whose neighbour is not Outside.
     unsigned bnd = 0;
     int cnt = 0;
 #pragma unroll
@@ -247,7 +260,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, co
     }
     const unsigned incl = warp_incl_scan_u((unsigned)cnt, lane);
     const int B = (int)__shfl_sync(FULL, incl, 31);
-    int q = (int)incl - cnt;
+    const int q0 = (int)incl - cnt;
     int nlive = 0;
     uint32_t fm[K];
 #pragma unroll
@@ -259,25 +272,41 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, co
     if (K == 8) fm[K - 1] &= 0x7FFFFFFFu;
     if (nlive + B > S_t::VUSE) return -ST_VCAP;
     const int f = C.np;
-    if (B <= 32) {
-        // One boundary edge per lane.  Owners list their edges at their
-        // prefix positions; every lane then reads its edge's data before any
-        // freed slot is reused.
-        {
-            int qq = q;
+    const int rounds = (B + 31) >> 5;
+    if (rounds > 1) {
+        // More than 32 new vertices (a cut through a large cell): make sure
+        // no Outside slot is reused before every round has read it.
+        int nfree_clean = 0;
 #pragma unroll
-            for (int k = 0; k < K; ++k)
+        for (int k = 0; k < K; ++k) nfree_clean += __popc(fm[k] & ~om[k]);
+        if (nfree_clean < B) return -ST_VCAP;
 #pragma unroll
-                for (int e = 0; e < 3; ++e)
-                    if (bnd & (1u << (3 * k + e))) S.item[qq++] = (uint16_t)((k * 32 + lane) | (e << 8));
-        }
-        __syncwarp();
-        const bool act = lane < B;
+        for (int k = 0; k < K; ++k) fm[k] &= ~om[k];
+    }
+    // Owners list their boundary edges (slot | edge << 8) at their prefix
+    // positions; lane l then places new vertex l (+ 32 per round).
+    uint16_t* items = S.items;
+    {
+        int qq = q0;
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+#pragma unroll
+            for (int e = 0; e < 3; ++e)
+                if (bnd & (1u << (3 * k + e))) items[qq++] = (uint16_t)((k * 32 + lane) | (e << 8));
+    }
+    __syncwarp();
+    uint32_t newm[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) newm[k] = 0;
+    bool bad = false;
+    for (int r0 = 0; r0 < B; r0 += 32) {
+        const int qi = r0 + lane;
+        const bool act = qi < B;
         int y = 0, a = 0, b = 0, slot = 0;
         uint32_t ty = 0;
-        T px = 0, py = 0, pz = 0;
+        T px = 0, py = 0, pz = 0, pe = 0;
         if (act) {
-            const uint32_t it = S.item[lane];
+            const uint32_t it = items[qi];
             const int x = it & 0xFF, e = it >> 8;
             const uint32_t xt_ = S.tri[x], xa_ = S.adj[x];
             a = plane_of(xt_, e);
@@ -288,17 +317,27 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, co
             ty = S.tri[y];
             // intersection(outside X, inside Y) (vector3.rs:213-219); an
             // Incident Y is kept as the new vertex (polyhedron.rs:554-565)
-            const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / (xsd - ysd);
+            const T den = xsd - ysd;
+            const T t = (!GUARD && ysd >= -(T)kTolerance) ? (T)1 : xsd / den;
             px = xx + (yx - xx) * t;
             py = xy + (yy - xy) * t;
             pz = xz + (yz - xz) * t;
-            slot = select_k<K>(fm, lane);
+            if constexpr (GUARD) {
+                // error bound of the new vertex: the endpoints' bounds plus the
+                // edge length times the error of t
+                const T ex = S.ve[x], ey = S.ve[y];
+                const T dl = fabs(yx - xx) + fabs(yy - xy) + fabs(yz - xz);
+                pe = max(ex, ey) + dl * (rn * (ex + ey + (T)2 * cR) / den) +
+                     (T)1.2e-7 * (fabs(px) + fabs(py) + fabs(pz));
+            }
+            slot = select_k<K>(fm, qi);
         }
         __syncwarp();
         if (act) {
             S.vx[slot] = px;
             S.vy[slot] = py;
             S.vz[slot] = pz;
+            if constexpr (GUARD) S.ve[slot] = pe;
             S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
             // Y's pointer back to X is the edge (b, a) of Y's triple.
             const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
@@ -307,126 +346,48 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, co
             reinterpret_cast<uint8_t*>(S.adj)[4 * y + yi] = (uint8_t)slot;
             S.mapf[a] = (uint8_t)slot;
             S.maps[b] = (uint8_t)slot;
+            S.adj[slot] = (uint32_t)y;
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if ((slot >> 5) == k) newm[k] |= 1u << (slot & 31);
         }
-        __syncwarp();
-        bool bad = false;
-        if (act) {
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < K; ++k) newm[k] = __reduce_or_sync(FULL, newm[k]);
+    // Link the ring of new vertices (each by its owner lane): across (b, f)
+    // lies the new vertex whose first plane is b, across (f, a) the one whose
+    // second plane is a.
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if ((newm[k] >> lane) & 1u) {
+            const int s = k * 32 + lane;
+            const uint32_t tt = S.tri[s];
+            const int a = plane_of(tt, 0), b = plane_of(tt, 1);
             const int n1 = S.mapf[b], n2 = S.maps[a];
-            bad = (S.mapf[a] != slot) || (S.maps[b] != slot) || n1 == 0xFF || n2 == 0xFF;
-            S.adj[slot] = (uint32_t)y | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
+            bad |= (S.mapf[a] != s) || (S.maps[b] != s) || n1 == 0xFF || n2 == 0xFF;
+            S.adj[s] = (S.adj[s] & 0xFFu) | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
         }
-        __syncwarp();
-        if (act) {
-            S.mapf[a] = 0xFF;
-            S.maps[b] = 0xFF;
-        }
-        if (__any_sync(FULL, bad)) return -ST_DEGEN;
-        uint32_t newm[K];
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            newm[k] = __reduce_or_sync(FULL, (act && (slot >> 5) == k) ? (1u << (slot & 31)) : 0u);
-            C.lm[k] = (C.lm[k] & ~om[k]) | newm[k];
-        }
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            if ((newm[k] >> lane) & 1u) {
-                const int s = k * 32 + lane;
-                C.vx[k] = S.vx[s];
-                C.vy[k] = S.vy[s];
-                C.vz[k] = S.vz[s];
-            }
-        }
-        if (lane == 0) {
-            S.px[f] = nx;
-            S.py[f] = ny;
-            S.pz[f] = nz;
-            S.pd[f] = off;
-            S.pid[f] = (int32_t)(sorted[src] - pt_base);
-            S.psrc[f] = src;
-        }
-        C.np = f + 1;
-        __syncwarp();
-        return 1;
-    }
-    __syncwarp();
-
-    // Pass 1: place the new vertices.
-    uint32_t newm[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) newm[k] = 0;
-    int nslot[3 * K], na[3 * K], nbp[3 * K], ny_[3 * K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-            const int c = 3 * k + e;
-            nslot[c] = -1;
-            if (bnd & (1u << c)) {
-                const int a = plane_of(xt[k], e);
-                const int b = plane_of(xt[k], (e + 1) % 3);
-                const int y = plane_of(xa[k], e);
-                const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
-                const T xsd = sd[k];
-                const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / (xsd - ysd);
-                const T px = C.vx[k] + (yx - C.vx[k]) * t;
-                const T py = C.vy[k] + (yy - C.vy[k]) * t;
-                const T pz = C.vz[k] + (yz - C.vz[k]) * t;
-                const int slot = select_k<K>(fm, q);
-                ++q;
-                S.vx[slot] = px;
-                S.vy[slot] = py;
-                S.vz[slot] = pz;
-                S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
-                // Y's pointer back to X is the edge (b, a) of Y's triple.
-                const uint32_t ty = S.tri[y];
-                const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
-                               : (plane_of(ty, 1) == b && plane_of(ty, 2) == a) ? 1
-                                                                                : 2;
-                reinterpret_cast<uint8_t*>(S.adj)[4 * y + yi] = (uint8_t)slot;
-                S.mapf[a] = (uint8_t)slot;
-                S.maps[b] = (uint8_t)slot;
-                set_k<K>(newm, slot);
-                nslot[c] = slot;
-                na[c] = a;
-                nbp[c] = b;
-                ny_[c] = y;
-            }
-        }
-    }
-    __syncwarp();
-    // Pass 2: link the ring of new vertices.
-    bool bad = false;
-#pragma unroll
-    for (int c = 0; c < 3 * K; ++c) {
-        if (nslot[c] >= 0) {
-            const int n1 = S.mapf[nbp[c]];
-            const int n2 = S.maps[na[c]];
-            bad |= (S.mapf[na[c]] != nslot[c]) || (S.maps[nbp[c]] != nslot[c]) || n1 == 0xFF || n2 == 0xFF;
-            S.adj[nslot[c]] = (uint32_t)ny_[c] | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
-        }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int c = 0; c < 3 * K; ++c) {
-        if (nslot[c] >= 0) {
-            S.mapf[na[c]] = 0xFF;
-            S.maps[nbp[c]] = 0xFF;
-        }
-    }
-    if (__any_sync(FULL, bad)) return -ST_DEGEN;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        newm[k] = __reduce_or_sync(FULL, newm[k]);
-        C.lm[k] = (C.lm[k] & ~om[k]) | newm[k];
     }
     __syncwarp();
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         if ((newm[k] >> lane) & 1u) {
+            const uint32_t tt = S.tri[k * 32 + lane];
+            S.mapf[plane_of(tt, 0)] = 0xFF;
+            S.maps[plane_of(tt, 1)] = 0xFF;
+        }
+    }
+    if (__any_sync(FULL, bad)) return -ST_DEGEN;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        C.lm[k] = (C.lm[k] & ~om[k]) | newm[k];
+        if ((newm[k] >> lane) & 1u) {
             const int s = k * 32 + lane;
             C.vx[k] = S.vx[s];
             C.vy[k] = S.vy[s];
             C.vz[k] = S.vz[s];
+            if constexpr (GUARD) C.ve[k] = S.ve[s];
         }
     }
     if (lane == 0) {
@@ -442,12 +403,22 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, co
     return 1;
 }
 
+// Squared radius of the cell about its site: max |v|^2 over live vertices;
+// in the FP32 form each |v| is inflated by its error bound.
 template <typename T, int K>
 __device__ __forceinline__ T live_r2(const CellRegs<T, K>& C, int lane) {
     T r2 = 0;
 #pragma unroll
-    for (int k = 0; k < K; ++k)
-        if ((C.lm[k] >> lane) & 1u) r2 = max(r2, C.vx[k] * C.vx[k] + C.vy[k] * C.vy[k] + C.vz[k] * C.vz[k]);
+    for (int k = 0; k < K; ++k) {
+        if ((C.lm[k] >> lane) & 1u) {
+            T q = C.vx[k] * C.vx[k] + C.vy[k] * C.vy[k] + C.vz[k] * C.vz[k];
+            if (sizeof(T) == 4) {
+                const T r = sqrt(q) + C.ve[k];
+                q = r * r;
+            }
+            r2 = max(r2, q);
+        }
+    }
     return warp_max_t(r2);
 }
 
@@ -524,6 +495,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         C.vx[k] = C.vy[k] = C.vz[k] = (T)0;
+        C.ve[k] = (T)0;
         C.lm[k] = 0;
     }
     C.lm[0] = 0xFFu;
@@ -548,6 +520,11 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         S.vx[lane] = C.vx[0];
         S.vy[lane] = C.vy[0];
         S.vz[lane] = C.vz[0];
+        if constexpr (GUARD) {
+            // rounding of the FP64 box corner to FP32
+            C.ve[0] = (T)1.2e-7 * (fabs(C.vx[0]) + fabs(C.vy[0]) + fabs(C.vz[0]));
+            S.ve[lane] = C.ve[0];
+        }
         const int pX = bx, pY = 2 + by, pZ = 4 + bz;
         const int sgn = (bx ? 1 : -1) * (by ? 1 : -1) * (bz ? 1 : -1);
         const int t0 = pX, t1 = sgn > 0 ? pY : pZ, t2 = sgn > 0 ? pZ : pY;
@@ -562,7 +539,8 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     }
     __syncwarp();
     T R2 = live_r2(C, lane);
-    T guard = (T)P.guard_rel * sqrt(R2);
+    // cR: bound on the FP32 rounding of one plane test, relative to the cell radius
+    T cR = (T)P.guard_rel * sqrt(R2);
     int status = ST_OK;
 
     // ---- the walk over bins in shell order (celery.rs:1023-1075) ----
@@ -650,13 +628,13 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     if (GUARD) break;   // sorted: every later candidate is as far
                     continue;
                 }
-                T nx, ny, nz, off;
-                bisector(cx, cy, cz, c2, nx, ny, nz, off);
-                const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, P.sorted, D.pt_base, cj, guard, lane);
+                T nx, ny, nz, off, rn;
+                bisector(cx, cy, cz, c2, nx, ny, nz, off, rn);
+                const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, rn, cR, P.sorted, D.pt_base, cj, lane);
                 if (r < 0) return -r;
                 if (r > 0) {
                     R2 = live_r2(C, lane);
-                    guard = (T)P.guard_rel * sqrt(R2);
+                    cR = (T)P.guard_rel * sqrt(R2);
                 }
             }
         }
@@ -824,7 +802,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     const float ddx = (ra * bcx + rb * cax + rc * abx) * inv;
                     const float ddy = (ra * bcy + rb * cay + rc * aby) * inv;
                     const float ddz = (ra * bcz + rb * caz + rc * abz) * inv;
-                    if (!(fabsf(ddx) <= vlim && fabsf(ddy) <= vlim && fabsf(ddz) <= vlim)) vbad = true;
+                    // the correction must stay within the vertex's error bound
+                    const float lim = 2.0f * C.ve[k] + vlim;
+                    if (!(fabsf(ddx) <= lim && fabsf(ddy) <= lim && fabsf(ddz) <= lim)) vbad = true;
                     S.dx[s] = ddx;
                     S.dy[s] = ddy;
                     S.dz[s] = ddz;
