@@ -49,13 +49,17 @@ namespace tess {
 namespace clipk {
 
 constexpr unsigned FULL = 0xffffffffu;
+// FP32 form: relative error constant of a vertex solved from its three planes
+// (a few FP32 roundings of the plane data and of Cramer's rule).
+constexpr float kVertexErr = 1.5e-6f;
 
 template <typename T, int K>
 struct Smem {
     static constexpr int V = 32 * K;                                 // vertex slots
     static constexpr int P = (32 * K + 32) < 254 ? (32 * K + 32) : 254;  // planes (< 0xFF)
     static constexpr int VUSE = V < 255 ? V : 255;                    // slot 255 is the map sentinel
-    T px[P], py[P], pz[P], pd[P];     // plane: unit normal, offset
+    T px[P], py[P], pz[P], pd[P];     // plane: normal, offset (n.x = offset)
+    T pn[P];                          // |normal| (1 for the FP64 form and the walls)
     T vx[V], vy[V], vz[V], vsd[V];    // vertex mirror, signed distances
     int32_t pid[P];                   // neighbour id (local original index) or wall code
     uint32_t psrc[P];                 // sorted index of the point that made the plane
@@ -317,18 +321,30 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             ty = S.tri[y];
             // intersection(outside X, inside Y) (vector3.rs:213-219); an
             // Incident Y is kept as the new vertex (polyhedron.rs:554-565)
-            const T den = xsd - ysd;
-            const T t = (!GUARD && ysd >= -(T)kTolerance) ? (T)1 : xsd / den;
-            px = xx + (yx - xx) * t;
-            py = xy + (yy - xy) * t;
-            pz = xz + (yz - xz) * t;
             if constexpr (GUARD) {
-                // error bound of the new vertex: the endpoints' bounds plus the
-                // edge length times the error of t
-                const T ex = S.ve[x], ey = S.ve[y];
-                const T dl = fabs(yx - xx) + fabs(yy - xy) + fabs(yz - xz);
-                pe = max(ex, ey) + dl * (rn * (ex + ey + (T)2 * cR) / den) +
-                     (T)1.2e-7 * (fabs(px) + fabs(py) + fabs(pz));
+                // FP32 form: the vertex of planes (a, b, f) by Cramer's rule,
+                // x = (h_a (n_b x n_f) + h_b (n_f x n_a) + h_f (n_a x n_b)) / det.
+                // Its error depends on its own conditioning only (not on the
+                // edge it came from): |dx| <~ c |x| / |det of unit normals|.
+                const T ax = S.px[a], ay = S.py[a], az = S.pz[a], ah = S.pd[a];
+                const T bx = S.px[b], by = S.py[b], bz = S.pz[b], bh = S.pd[b];
+                const T bfx = by * nz - bz * ny, bfy = bz * nx - bx * nz, bfz = bx * ny - by * nx;
+                const T fax = ny * az - nz * ay, fay = nz * ax - nx * az, faz = nx * ay - ny * ax;
+                const T abx = ay * bz - az * by, aby = az * bx - ax * bz, abz = ax * by - ay * bx;
+                const T det = ax * bfx + ay * bfy + az * bfz;
+                const T inv = (T)1 / det;
+                px = (ah * bfx + bh * fax + off * abx) * inv;
+                py = (ah * bfy + bh * fay + off * aby) * inv;
+                pz = (ah * bfz + bh * faz + off * abz) * inv;
+                const T dhat = fabs(det) / (S.pn[a] * S.pn[b] * rn);
+                pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) / max(dhat, (T)1e-30);
+                if (!(pe < (T)1e30)) pe = (T)1e30;
+            } else {
+                const T den = xsd - ysd;
+                const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / den;
+                px = xx + (yx - xx) * t;
+                py = xy + (yy - xy) * t;
+                pz = xz + (yz - xz) * t;
             }
             slot = select_k<K>(fm, qi);
         }
@@ -395,6 +411,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         S.py[f] = ny;
         S.pz[f] = nz;
         S.pd[f] = off;
+        S.pn[f] = rn;
         S.pid[f] = (int32_t)(sorted[src] - pt_base);
         S.psrc[f] = src;
     }
@@ -510,6 +527,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         S.py[lane] = a == 1 ? sg : (T)0;
         S.pz[lane] = a == 2 ? sg : (T)0;
         S.pd[lane] = (T)off;
+        S.pn[lane] = (T)1;
         S.pid[lane] = -1 - lane;   // -1 x_min, -2 x_max, -3 y_min, -4 y_max, -5 z_min, -6 z_max
     }
     if (lane < 8) {
