@@ -56,7 +56,8 @@ typedef enum {
 } tess_precision;
 
 /* Flags for tess_config.flags */
-#define TESS_FLAG_TIMING 1u   /* record per-pass device times (tess_stats) */
+#define TESS_FLAG_TIMING 1u     /* record per-pass device times (tess_stats)          */
+#define TESS_FLAG_COUNTERS 2u   /* count the clipping work (tess_stats, small overhead) */
 
 typedef struct {
     /* FP32 form, guard band: a plane test of vertex v is undecided (the cell
@@ -98,6 +99,12 @@ typedef struct {
     uint64_t rerun_guard;       /* ... of them: a plane test inside the guard band */
     uint64_t rerun_verify;      /* ... FP32 vertex too far from its FP64 position   */
     uint64_t rerun_degenerate;  /* ... inconsistent topology                        */
+    /* work counters, with TESS_FLAG_COUNTERS (all passes): */
+    uint64_t candidates_tested; /* bisectors tested against the cell               */
+    uint64_t cuts;              /* bisectors that cut vertices off                 */
+    uint64_t new_vertices;      /* vertices created by the cuts                    */
+    uint64_t windows;           /* candidate windows of up to 32 points            */
+    uint64_t batches;           /* batches of up to 32 bins                        */
 } tess_stats;
 
 void tess_config_default(tess_config* cfg);

@@ -114,6 +114,7 @@ struct Engine {
     unsigned long long* d_fcursor = nullptr;
     uint32_t* d_list[L_COUNT] = {};
     unsigned* d_counters = nullptr;   // [0..15] cursors, [16..31] list counts
+    unsigned long long* d_work = nullptr;  // work counters (TESS_FLAG_COUNTERS)
     uint64_t* d_offs = nullptr;
     int32_t* d_cnbr = nullptr;
     double* d_carea = nullptr;
@@ -146,7 +147,7 @@ struct Engine {
         dfree(d_table); dfree(d_err); dfree(d_vol); dfree(d_nface); dfree(d_fstart); dfree(d_status);
         dfree(d_fnbr); dfree(d_farea); dfree(d_fcursor);
         for (auto& l : d_list) dfree(l);
-        dfree(d_counters); dfree(d_offs); dfree(d_cnbr); dfree(d_carea); dfree(d_csr_tmp);
+        dfree(d_counters); dfree(d_work); dfree(d_offs); dfree(d_cnbr); dfree(d_carea); dfree(d_csr_tmp);
         dfree(d_geo); dfree(d_one);
         if (own_stream && stream) cudaStreamDestroy(stream);
         stream = nullptr;
@@ -283,6 +284,7 @@ tess_status engine_init(Engine& E, const tess_config* cfg, std::vector<DiagDesc>
     TRY(dalloc(&E.d_fcursor, 1));
     for (auto& l : E.d_list) TRY(dalloc(&l, n));
     TRY(dalloc(&E.d_counters, 32));
+    TRY(dalloc(&E.d_work, 8));
     TRY(dalloc(&E.d_offs, n + 1));
     TRY(dalloc(&E.d_csr_tmp, csr_tmp_words(E.total)));
     TRY(dalloc(&E.d_geo, 1));
@@ -389,6 +391,7 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
     unsigned* cnt = E.d_counters + 16;
     CU(cudaMemsetAsync(E.d_counters, 0, sizeof(unsigned) * 32, E.stream));
     CU(cudaMemsetAsync(E.d_fcursor, 0, sizeof(unsigned long long), E.stream));
+    if (E.cfg.flags & TESS_FLAG_COUNTERS) CU(cudaMemsetAsync(E.d_work, 0, sizeof(unsigned long long) * 8, E.stream));
     ClipParams base = base_params(E);
     base.search_radius = radius;
     base.target_group = group;
@@ -406,6 +409,7 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         p.list_cap_count = ccap;
         p.fail_count = cnt + L_FAIL;
         p.reasons = cnt + L_REASON;
+        p.work_ctr = (E.cfg.flags & TESS_FLAG_COUNTERS) ? E.d_work : nullptr;
         CU(launch_clip(p, prec, slots, E.wpb_for(prec, slots), E.blocks(prec, slots), E.stream));
         E.launches += 1;
         return TESS_OK;
@@ -497,6 +501,15 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
         E.last_group = group;
         const uint64_t failed = counts[L_FAIL];
         E.stats.failed = failed;
+        if (E.cfg.flags & TESS_FLAG_COUNTERS) {
+            unsigned long long w[8];
+            CU(cudaMemcpy(w, E.d_work, sizeof(w), cudaMemcpyDeviceToHost));
+            E.stats.candidates_tested = w[0];
+            E.stats.cuts = w[1];
+            E.stats.new_vertices = w[2];
+            E.stats.windows = w[3];
+            E.stats.batches = w[4];
+        }
         E.stats.rerun_guard = counts[L_REASON + ST_GUARD];
         E.stats.rerun_verify = counts[L_REASON + ST_VERIFY];
         E.stats.rerun_degenerate = counts[L_REASON + ST_DEGEN];

@@ -179,6 +179,11 @@ __device__ __forceinline__ void bisector(double rx, double ry, double rz, double
 __device__ __forceinline__ float round_up_f(float x) { return x; }
 __device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
 
+// Per-warp work counters (reported when ClipParams::work is set).
+struct Work {
+    unsigned tested = 0, cuts = 0, newv = 0, windows = 0, batches = 0;
+};
+
 template <typename T, int K>
 struct CellRegs {
     T vx[K], vy[K], vz[K];
@@ -417,7 +422,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
     }
     C.np = f + 1;
     __syncwarp();
-    return 1;
+    return B + 1;
 }
 
 // Squared radius of the cell about its site: max |v|^2 over live vertices;
@@ -463,7 +468,7 @@ __device__ __forceinline__ void ring_offset(int s, uint32_t r, int& i, int& j, i
 }
 
 template <typename T, int K, bool GEO>
-__device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int lane) {
+__device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int lane, Work& W) {
     using S_t = Smem<T, K>;
     constexpr bool GUARD = sizeof(T) == 4;
     // ---- diagram of this cell ----
@@ -583,6 +588,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         S.cbeg[lane] = beg;
         __syncwarp();
         for (unsigned w0 = 0; w0 < total; w0 += 32) {
+            ++W.windows;
             const unsigned c = w0 + lane;
             bool keep = false;
             T rx = 0, ry = 0, rz = 0, r2 = 0;
@@ -649,8 +655,11 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 T nx, ny, nz, off, rn;
                 bisector(cx, cy, cz, c2, nx, ny, nz, off, rn);
                 const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, rn, cR, P.sorted, D.pt_base, cj, lane);
+                ++W.tested;
                 if (r < 0) return -r;
                 if (r > 0) {
+                    ++W.cuts;
+                    W.newv += (unsigned)(r - 1);
                     R2 = live_r2(C, lane);
                     cR = (T)P.guard_rel * sqrt(R2);
                 }
@@ -689,6 +698,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         long long lb = -1;
         if (lane < nval) lb = bin_of(oi, oj, ok);
         t += nval;
+        ++W.batches;
         status = process(lb);
         if (status != ST_OK) break;
         if (sm) {
@@ -716,6 +726,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     if (key > D.tab_kmax && key < thr && !(radius >= 0.0 && key > radius)) lb = bin_of(i, j, k);
                 }
                 if (!__any_sync(FULL, lb >= 0)) continue;
+                ++W.batches;
                 status = process(lb);
                 if (status != ST_OK) break;
             }
@@ -1043,6 +1054,7 @@ __global__ void k_clip(ClipParams P) {
     extern __shared__ __align__(16) unsigned char smraw[];
     Smem<T, K>& S = reinterpret_cast<Smem<T, K>*>(smraw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
+    Work W;
     for (;;) {
         unsigned w = 0;
         if (lane == 0) w = atomicAdd(P.cursor, 1u);
@@ -1050,7 +1062,14 @@ __global__ void k_clip(ClipParams P) {
         const unsigned total = P.work_count ? *P.work_count : P.total;
         if (w >= total) break;
         const uint32_t gs = P.work ? P.work[w] : w;
-        run_cell<T, K, GEO>(P, S, gs, lane);
+        run_cell<T, K, GEO>(P, S, gs, lane, W);
+    }
+    if (P.work_ctr && lane == 0) {
+        atomicAdd(&P.work_ctr[0], (unsigned long long)W.tested);
+        atomicAdd(&P.work_ctr[1], (unsigned long long)W.cuts);
+        atomicAdd(&P.work_ctr[2], (unsigned long long)W.newv);
+        atomicAdd(&P.work_ctr[3], (unsigned long long)W.windows);
+        atomicAdd(&P.work_ctr[4], (unsigned long long)W.batches);
     }
 }
 

@@ -176,6 +176,7 @@ struct ClipParams {
     unsigned int* list_cap_count;
     unsigned int* fail_count;     // cells left with an error status
     unsigned int* reasons;        // per status code: cells routed or failed for it
+    unsigned long long* work_ctr; // optional work counters (tested, cuts, new vertices, windows, batches)
     // options
     double search_radius;         // < 0: none
     int64_t target_group;         // < 0: none

@@ -30,11 +30,11 @@ from typing import List, Optional
 
 import numpy as np
 
-from ._capi import (FLAG_TIMING, PRECISION_FP32_GUARD, PRECISION_FP64, CellGeometry, Config, Stats,
+from ._capi import (FLAG_COUNTERS, FLAG_TIMING, PRECISION_FP32_GUARD, PRECISION_FP64, CellGeometry, Config, Stats,
                     TessError, check, default_config, last_error, lib)
 
 __all__ = ["Polyhedron", "Diagram", "Cell", "VoronoiFace", "Batch", "TessError", "Config",
-           "default_config", "PRECISION_FP64", "PRECISION_FP32_GUARD", "FLAG_TIMING", "lib",
+           "default_config", "PRECISION_FP64", "PRECISION_FP32_GUARD", "FLAG_TIMING", "FLAG_COUNTERS", "lib",
            "last_error"]
 
 _PREC = {"fp64": PRECISION_FP64, "fp32": PRECISION_FP32_GUARD, "fp32_guard": PRECISION_FP32_GUARD,

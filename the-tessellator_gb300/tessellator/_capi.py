@@ -17,6 +17,7 @@ STATUS_NAMES = {0: "TESS_OK", 1: "TESS_E_INVALID", 2: "TESS_E_CUDA", 3: "TESS_E_
                 4: "TESS_E_OVERFLOW", 5: "TESS_E_STATE", 6: "TESS_E_NOMEM", 7: "TESS_E_LIMIT"}
 PRECISION_FP64, PRECISION_FP32_GUARD = 0, 1
 FLAG_TIMING = 1
+FLAG_COUNTERS = 2
 MAX_CELL_VERTICES, MAX_CELL_FACES = 255, 254
 
 # Every function the header declares, in header order.
@@ -45,7 +46,9 @@ class Stats(C.Structure):
                 ("rerun_capacity", C.c_uint64), ("failed", C.c_uint64),
                 ("table_entries", C.c_uint64), ("ms_grid", C.c_double), ("ms_clip", C.c_double),
                 ("ms_rerun", C.c_double), ("ms_csr", C.c_double), ("launches", C.c_uint64),
-                ("rerun_guard", C.c_uint64), ("rerun_verify", C.c_uint64), ("rerun_degenerate", C.c_uint64)]
+                ("rerun_guard", C.c_uint64), ("rerun_verify", C.c_uint64), ("rerun_degenerate", C.c_uint64),
+                ("candidates_tested", C.c_uint64), ("cuts", C.c_uint64), ("new_vertices", C.c_uint64),
+                ("windows", C.c_uint64), ("batches", C.c_uint64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
