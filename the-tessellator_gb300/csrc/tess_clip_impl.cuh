@@ -615,41 +615,26 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 keep = (j != self) && r2 > (T)0 && r2 < lim;
                 if (keep && tgroup >= 0) keep = (int64_t)(P.sgroup ? P.sgroup[j] : 0u) == tgroup;
             }
-            const int nkeep = __popc(__ballot_sync(FULL, keep));
-            if (nkeep == 0) continue;
-            // Nearest first: a bitonic sort of the window by distance (ties by
-            // lane) lets the closest bisectors shrink the cell before the
-            // farther ones are tested.
-            int order = lane;
-            if (nkeep > 1) {
-                float key = keep ? (float)r2 : INFINITY;
-#pragma unroll
-                for (int k2 = 2; k2 <= 32; k2 <<= 1) {
-#pragma unroll
-                    for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
-                        const float ok = __shfl_xor_sync(FULL, key, j2);
-                        const int oi = __shfl_xor_sync(FULL, order, j2);
-                        const bool asc = (lane & k2) == 0;
-                        const bool lower = (lane & j2) == 0;
-                        const bool other_less = ok < key || (ok == key && oi < order);
-                        if (other_less == (lower == asc)) {
-                            key = ok;
-                            order = oi;
-                        }
-                    }
-                }
-            } else {
-                order = __ffs(__ballot_sync(FULL, keep)) - 1;
-            }
-            for (int q = 0; q < nkeep; ++q) {
-                const int src = __shfl_sync(FULL, order, q);
+            unsigned km = __ballot_sync(FULL, keep);
+            // Nearest first: repeatedly take the closest remaining candidate
+            // (warp minimum of its distance, ties by lane), so the closest
+            // bisectors shrink the cell before the farther ones are tested.
+            // The key keeps the top 27 bits of r2 (a positive float orders
+            // like its bits) and the lane in the low 5.
+            const unsigned mykey = (__float_as_uint((float)r2) & ~31u) | (unsigned)lane;
+            while (km) {
+                const unsigned best = __reduce_min_sync(FULL, ((km >> lane) & 1u) ? mykey : 0xFFFFFFFFu);
+                const int src = (int)(best & 31u);
+                km &= ~(1u << src);
                 const T cx = __shfl_sync(FULL, rx, src);
                 const T cy = __shfl_sync(FULL, ry, src);
                 const T cz = __shfl_sync(FULL, rz, src);
                 const T c2 = __shfl_sync(FULL, r2, src);
                 const uint32_t cj = __shfl_sync(FULL, j, src);
-                if (!(c2 < (T)4 * R2 * (T)kStopMargin)) {
-                    if (GUARD) break;   // sorted: every later candidate is as far
+                const T lim2 = (T)4 * R2 * (T)kStopMargin;
+                if (!(c2 < lim2)) {
+                    // taken in increasing distance: the rest are farther still
+                    if (c2 > lim2 * (T)1.001) km = 0;
                     continue;
                 }
                 T nx, ny, nz, off, rn;
@@ -669,9 +654,33 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         return ST_OK;
     };
 
+    // The site's fractional position inside its bin, for a tighter per-bin
+    // test than the gap key: a point of bin (b + o) lies at least
+    // |o| - 1 + f (o < 0) or o - f (o > 0) bin sides from the site on each
+    // axis.  Off-grid sites (cells of external points) skip the test.
+    const float fx = (float)(__dmul_rn(sx - D.glo[0], D.inv[0]) - (double)cbx);
+    const float fy = (float)(__dmul_rn(sy - D.glo[1], D.inv[1]) - (double)cby);
+    const float fz = (float)(__dmul_rn(sz - D.glo[2], D.inv[2]) - (double)cbz);
+    const bool near_ok = fx >= -1e-3f && fx <= 1.001f && fy >= -1e-3f && fy <= 1.001f && fz >= -1e-3f &&
+                         fz <= 1.001f && D.min_size > 0.0;
+    const float bsx = (float)D.size[0], bsy = (float)D.size[1], bsz = (float)D.size[2];
+    // squared distance (bin units scaled by the bin sides) from the site to
+    // the nearest point of the bin at offset (i, j, k)
+    auto near2 = [&](int i, int j, int k) -> float {
+        const float fxc = fminf(fmaxf(fx, 0.f), 1.f), fyc = fminf(fmaxf(fy, 0.f), 1.f),
+                    fzc = fminf(fmaxf(fz, 0.f), 1.f);
+        const float dx = i > 0 ? (float)i - fxc : (i < 0 ? (float)(-i - 1) + fxc : 0.f);
+        const float dy = j > 0 ? (float)j - fyc : (j < 0 ? (float)(-j - 1) + fyc : 0.f);
+        const float dz = k > 0 ? (float)k - fzc : (k < 0 ? (float)(-k - 1) + fzc : 0.f);
+        const float ax = dx * bsx, ay = dy * bsy, az = dz * bsz;
+        return ax * ax + ay * ay + az * az;
+    };
     auto bin_of = [&](int i, int j, int k) -> long long {
         const int x = cbx + i, y = cby + j, z = cbz + k;
         if (x < 0 || x >= cpd || y < 0 || y >= cpd || z < 0 || z >= cpd) return -1;
+        // no point of this bin can cut: it lies beyond twice the cell radius
+        if (near_ok && near2(i, j, k) * (1.0f - 1e-4f) >= (float)(4.0 * (double)R2))
+            return -1;
         return (long long)(D.bin_base + ((uint64_t)x * cpd + y) * cpd + z);
     };
 
