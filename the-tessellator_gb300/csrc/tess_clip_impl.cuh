@@ -67,6 +67,7 @@ struct Smem {
     uint32_t adj[V];                  // neighbours n0 | n1 << 8 | n2 << 16
     uint32_t fdeg[P];                 // finalize: live vertices per face
     uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
+    uint32_t cbeg2[32], ccnt[32];     // second bin of each lane: start; first bin's count
     uint16_t items[V + 32];           // boundary edges of a cut: slot | edge << 8
     int32_t flist[P];                 // finalize: compacted face ids
     uint8_t fsta[P];                  // finalize: one vertex of each face
@@ -575,17 +576,16 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     const int64_t tgroup = P.target_group;
     const TabEntry* tab = P.table + D.tab_base;
 
-    // Cut by every point of the lane's bin (lb = global bin, or -1).
-    auto process = [&](long long lb) -> int {
-        unsigned cnt = 0, beg = 0;
-        if (lb >= 0) {
-            beg = P.delims[lb];
-            cnt = P.delims[lb + 1] - beg;
-        }
+    // Cut by every point of the lane's two bins, given as sorted ranges
+    // [begA, begA + cntA) and [begB, begB + cntB).
+    auto process = [&](unsigned begA, unsigned cntA, unsigned begB, unsigned cntB) -> int {
+        const unsigned cnt = cntA + cntB;
         const unsigned incl = warp_incl_scan_u(cnt, lane);
         const unsigned total = __shfl_sync(FULL, incl, 31);
         S.cpref[lane] = incl - cnt;
-        S.cbeg[lane] = beg;
+        S.cbeg[lane] = begA;
+        S.cbeg2[lane] = begB;
+        S.ccnt[lane] = cntA;
         __syncwarp();
         for (unsigned w0 = 0; w0 < total; w0 += 32) {
             ++W.windows;
@@ -601,7 +601,8 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     if (S.cpref[mid] <= c) lo = mid;
                     else hi = mid - 1;
                 }
-                j = S.cbeg[lo] + (c - S.cpref[lo]);
+                const unsigned o = c - S.cpref[lo], na = S.ccnt[lo];
+                j = o < na ? S.cbeg[lo] + o : S.cbeg2[lo] + (o - na);
                 if constexpr (GUARD) {
                     rx = (T)((P.shi[3ull * j] - shx) + (P.slo[3ull * j] - slx));
                     ry = (T)((P.shi[3ull * j + 1] - shy) + (P.slo[3ull * j + 1] - sly));
@@ -684,33 +685,63 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         return (long long)(D.bin_base + ((uint64_t)x * cpd + y) * cpd + z);
     };
 
-    // phase 1: the sorted shell table
+    // phase 1: the sorted shell table, 64 entries per batch (two per lane:
+    // entry t + lane and entry t + 32 + lane).  The next batch's table
+    // entries and bin ranges are loaded before the current batch's points are
+    // cut, so their latency overlaps the cutting.
     bool phase2 = false;
     uint32_t t = 0;
+    // a batch entry: offsets, key and, after the bin test, the sorted range
+    struct Ent {
+        int i, j, k;
+        float key;
+        unsigned beg, cnt;
+    };
+    auto load_entry = [&](uint32_t idx, Ent& e) {
+        e.i = e.j = e.k = 0;
+        e.key = INFINITY;
+        e.beg = e.cnt = 0;
+        if (idx < D.tab_len) {
+            const TabEntry te = tab[idx];
+            e.i = te.i;
+            e.j = te.j;
+            e.k = te.k;
+            e.key = te.key;
+            if (radius >= 0.0 && gap_key(D.size, e.i, e.j, e.k) > radius) e.key = INFINITY;
+            const long long lb = bin_of(e.i, e.j, e.k);
+            if (lb >= 0) {
+                e.beg = P.delims[lb];
+                e.cnt = P.delims[lb + 1] - e.beg;
+            }
+        }
+    };
+    Ent ea, eb;
+    load_entry(lane, ea);
+    load_entry(32 + lane, eb);
     for (;;) {
         // The table key is rounded toward zero and the threshold up, so
         // stopping on key >= thr never drops a bin that could hold a cutter.
         const float thr = round_up_f((T)4 * R2 * (T)kStopMargin);
-        const uint32_t idx = t + lane;
-        bool stop = true;
-        int oi = 0, oj = 0, ok = 0;
-        if (idx < D.tab_len) {
-            const TabEntry e = tab[idx];
-            oi = e.i;
-            oj = e.j;
-            ok = e.k;
-            stop = !(e.key < thr);
-            if (radius >= 0.0) stop = stop || gap_key(D.size, oi, oj, ok) > radius;
+        const bool sa = !(ea.key < thr), sb = !(eb.key < thr);
+        const unsigned ma = __ballot_sync(FULL, sa), mb = __ballot_sync(FULL, sb);
+        const int na = ma ? __ffs(ma) - 1 : 32;
+        const int nb = ma ? 0 : (mb ? __ffs(mb) - 1 : 32);
+        unsigned ba = ea.beg, ca = lane < na ? ea.cnt : 0u;
+        unsigned bb = eb.beg, cb = lane < nb ? eb.cnt : 0u;
+        // re-test the bins against the current (smaller) radius
+        if (ca && near_ok && near2(ea.i, ea.j, ea.k) * (1.0f - 1e-4f) >= (float)(4.0 * (double)R2)) ca = 0;
+        if (cb && near_ok && near2(eb.i, eb.j, eb.k) * (1.0f - 1e-4f) >= (float)(4.0 * (double)R2)) cb = 0;
+        const bool last = (ma | mb) != 0;
+        const uint32_t used = (uint32_t)(na + nb);
+        t += used;
+        if (!last) {
+            load_entry(t + lane, ea);
+            load_entry(t + 32 + lane, eb);
         }
-        const unsigned sm = __ballot_sync(FULL, stop);
-        const int nval = sm ? __ffs(sm) - 1 : 32;
-        long long lb = -1;
-        if (lane < nval) lb = bin_of(oi, oj, ok);
-        t += nval;
         ++W.batches;
-        status = process(lb);
+        status = process(ba, ca, bb, cb);
         if (status != ST_OK) break;
-        if (sm) {
+        if (last) {
             phase2 = (t >= D.tab_len) && isfinite(D.tab_kmax);
             break;
         }
@@ -736,7 +767,12 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 }
                 if (!__any_sync(FULL, lb >= 0)) continue;
                 ++W.batches;
-                status = process(lb);
+                unsigned beg = 0, cnt = 0;
+                if (lb >= 0) {
+                    beg = P.delims[lb];
+                    cnt = P.delims[lb + 1] - beg;
+                }
+                status = process(beg, cnt, 0u, 0u);
                 if (status != ST_OK) break;
             }
         }
