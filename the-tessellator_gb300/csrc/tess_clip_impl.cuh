@@ -67,7 +67,7 @@ struct Smem {
     uint32_t adj[V];                  // neighbours n0 | n1 << 8 | n2 << 16
     uint32_t fdeg[P];                 // finalize: live vertices per face
     uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
-    uint32_t cbeg2[32], ccnt[32];     // second bin of each lane: start; first bin's count
+    uint32_t cbeg2[32], ccnt[32];     // second-half bins: starts and prefix counts
     uint16_t items[V + 32];           // boundary edges of a cut: slot | edge << 8
     int32_t flist[P];                 // finalize: compacted face ids
     uint8_t fsta[P];                  // finalize: one vertex of each face
@@ -579,13 +579,16 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     // Cut by every point of the lane's two bins, given as sorted ranges
     // [begA, begA + cntA) and [begB, begB + cntB).
     auto process = [&](unsigned begA, unsigned cntA, unsigned begB, unsigned cntB) -> int {
-        const unsigned cnt = cntA + cntB;
-        const unsigned incl = warp_incl_scan_u(cnt, lane);
-        const unsigned total = __shfl_sync(FULL, incl, 31);
-        S.cpref[lane] = incl - cnt;
+        // candidate order: every first-half bin (nearer in the table) before
+        // every second-half bin
+        const unsigned inca = warp_incl_scan_u(cntA, lane);
+        const unsigned incb = warp_incl_scan_u(cntB, lane);
+        const unsigned totala = __shfl_sync(FULL, inca, 31);
+        const unsigned total = totala + __shfl_sync(FULL, incb, 31);
+        S.cpref[lane] = inca - cntA;
         S.cbeg[lane] = begA;
+        S.ccnt[lane] = totala + incb - cntB;   // prefix of the second-half bins
         S.cbeg2[lane] = begB;
-        S.ccnt[lane] = cntA;
         __syncwarp();
         for (unsigned w0 = 0; w0 < total; w0 += 32) {
             ++W.windows;
@@ -595,14 +598,15 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             uint32_t j = 0;
             const T lim = (T)4 * R2 * (T)kStopMargin;
             if (c < total) {
+                const bool second = c >= totala;
+                const uint32_t* pref = second ? S.ccnt : S.cpref;
                 int lo = 0, hi = 31;
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
-                    if (S.cpref[mid] <= c) lo = mid;
+                    if (pref[mid] <= c) lo = mid;
                     else hi = mid - 1;
                 }
-                const unsigned o = c - S.cpref[lo], na = S.ccnt[lo];
-                j = o < na ? S.cbeg[lo] + o : S.cbeg2[lo] + (o - na);
+                j = (second ? S.cbeg2[lo] : S.cbeg[lo]) + (c - pref[lo]);
                 if constexpr (GUARD) {
                     rx = (T)((P.shi[3ull * j] - shx) + (P.slo[3ull * j] - slx));
                     ry = (T)((P.shi[3ull * j + 1] - shy) + (P.slo[3ull * j + 1] - sly));
