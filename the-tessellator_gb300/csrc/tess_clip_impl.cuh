@@ -52,6 +52,8 @@ constexpr unsigned FULL = 0xffffffffu;
 // FP32 form: relative error constant of a vertex solved from its three planes
 // (a few FP32 roundings of the plane data and of Cramer's rule).
 constexpr float kVertexErr = 1.5e-6f;
+// Shell-table entries per walk batch: 32 (one per lane) or 64 (two per lane).
+constexpr bool kBatch2 = false;
 
 template <typename T, int K>
 struct Smem {
@@ -204,8 +206,8 @@ struct CellRegs {
 // Returns 1 when vertices were cut off, 0 when nothing was Outside, or
 // -status.
 template <typename T, int K, bool GUARD>
-__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T rn, T cR,
-                   const uint32_t* sorted, uint32_t pt_base, uint32_t src, int lane) {
+__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T rn, T cR, int32_t id,
+                   uint32_t src, int lane) {
     using S_t = Smem<T, K>;
     T sd[K];
     uint32_t om[K];
@@ -418,7 +420,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         S.pz[f] = nz;
         S.pd[f] = off;
         S.pn[f] = rn;
-        S.pid[f] = (int32_t)(sorted[src] - pt_base);
+        S.pid[f] = id;
         S.psrc[f] = src;
     }
     C.np = f + 1;
@@ -484,6 +486,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         d = lo;
     }
     const DiagDesc& D = P.diags[d];
+    const uint32_t pt_base = D.pt_base;
+    const uint64_t bin_base = D.bin_base;
+    const uint32_t tab_len = D.tab_len;
     double sx, sy, sz;
     uint32_t self = 0xFFFFFFFFu, orig = 0;
     if (P.at_point) {
@@ -596,6 +601,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             bool keep = false;
             T rx = 0, ry = 0, rz = 0, r2 = 0;
             uint32_t j = 0;
+            int32_t cid = 0;
             const T lim = (T)4 * R2 * (T)kStopMargin;
             if (c < total) {
                 const bool second = c >= totala;
@@ -618,6 +624,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 }
                 r2 = rx * rx + ry * ry + rz * rz;
                 keep = (j != self) && r2 > (T)0 && r2 < lim;
+                cid = (int32_t)(P.sorted[j] - pt_base);
                 if (keep && tgroup >= 0) keep = (int64_t)(P.sgroup ? P.sgroup[j] : 0u) == tgroup;
             }
             unsigned km = __ballot_sync(FULL, keep);
@@ -636,6 +643,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 const T cz = __shfl_sync(FULL, rz, src);
                 const T c2 = __shfl_sync(FULL, r2, src);
                 const uint32_t cj = __shfl_sync(FULL, j, src);
+                const int32_t cidb = __shfl_sync(FULL, cid, src);
                 const T lim2 = (T)4 * R2 * (T)kStopMargin;
                 if (!(c2 < lim2)) {
                     // taken in increasing distance: the rest are farther still
@@ -644,7 +652,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 }
                 T nx, ny, nz, off, rn;
                 bisector(cx, cy, cz, c2, nx, ny, nz, off, rn);
-                const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, rn, cR, P.sorted, D.pt_base, cj, lane);
+                const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, rn, cR, cidb, cj, lane);
                 ++W.tested;
                 if (r < 0) return -r;
                 if (r > 0) {
@@ -686,7 +694,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         // no point of this bin can cut: it lies beyond twice the cell radius
         if (near_ok && near2(i, j, k) * (1.0f - 1e-4f) >= (float)(4.0 * (double)R2))
             return -1;
-        return (long long)(D.bin_base + ((uint64_t)x * cpd + y) * cpd + z);
+        return (long long)(bin_base + ((uint64_t)x * cpd + y) * cpd + z);
     };
 
     // phase 1: the sorted shell table, 64 entries per batch (two per lane:
@@ -705,7 +713,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         e.i = e.j = e.k = 0;
         e.key = INFINITY;
         e.beg = e.cnt = 0;
-        if (idx < D.tab_len) {
+        if (idx < tab_len) {
             const TabEntry te = tab[idx];
             e.i = te.i;
             e.j = te.j;
@@ -720,16 +728,19 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         }
     };
     Ent ea, eb;
+    eb.i = eb.j = eb.k = 0;
+    eb.key = INFINITY;
+    eb.beg = eb.cnt = 0;
     load_entry(lane, ea);
-    load_entry(32 + lane, eb);
+    if (kBatch2) load_entry(32 + lane, eb);
     for (;;) {
         // The table key is rounded toward zero and the threshold up, so
         // stopping on key >= thr never drops a bin that could hold a cutter.
         const float thr = round_up_f((T)4 * R2 * (T)kStopMargin);
-        const bool sa = !(ea.key < thr), sb = !(eb.key < thr);
+        const bool sa = !(ea.key < thr), sb = kBatch2 && !(eb.key < thr);
         const unsigned ma = __ballot_sync(FULL, sa), mb = __ballot_sync(FULL, sb);
         const int na = ma ? __ffs(ma) - 1 : 32;
-        const int nb = ma ? 0 : (mb ? __ffs(mb) - 1 : 32);
+        const int nb = (ma || !kBatch2) ? 0 : (mb ? __ffs(mb) - 1 : 32);
         unsigned ba = ea.beg, ca = lane < na ? ea.cnt : 0u;
         unsigned bb = eb.beg, cb = lane < nb ? eb.cnt : 0u;
         // re-test the bins against the current (smaller) radius
@@ -740,13 +751,13 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         t += used;
         if (!last) {
             load_entry(t + lane, ea);
-            load_entry(t + 32 + lane, eb);
+            if (kBatch2) load_entry(t + 32 + lane, eb);
         }
         ++W.batches;
         status = process(ba, ca, bb, cb);
         if (status != ST_OK) break;
         if (last) {
-            phase2 = (t >= D.tab_len) && isfinite(D.tab_kmax);
+            phase2 = (t >= tab_len) && isfinite(D.tab_kmax);
             break;
         }
     }
