@@ -71,6 +71,7 @@ struct Smem {
     uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
     uint32_t cbeg2[32], ccnt[32];     // second-half bins: starts and prefix counts
     uint16_t items[V + 32];           // boundary edges of a cut: slot | edge << 8
+    uint8_t fl[V + 32];               // free-slot stack (top = lowest free slot)
     int32_t flist[P];                 // finalize: compacted face ids
     uint8_t fsta[P];                  // finalize: one vertex of each face
     uint8_t mapf[P], maps[P];         // new-vertex ring maps
@@ -193,6 +194,7 @@ struct CellRegs {
     T ve[K];          // FP32 form: bound on each vertex's position error
     uint32_t lm[K];   // live masks (warp-uniform)
     int np;           // planes used (warp-uniform)
+    int nfree;        // entries on the free-slot stack (warp-uniform)
 };
 
 // Clip the cell by the half-space {x : n.x - off <= 0}.
@@ -226,6 +228,130 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
     for (int k = 0; k < K; ++k) anyo |= om[k];
     if (!anyo) return 0;
     if (C.np >= S_t::P) return -ST_PCAP;
+    int R = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) R += __popc(om[k]);
+    if (3 * R <= 32) {
+        // Fast path: one lane per edge of an Outside vertex.  The Outside
+        // slots are pushed onto the free-slot stack; the new vertices pop
+        // slots from its top (reusing freed slots first).
+        const int f = C.np;
+        const int base = C.nfree;
+        int before = 0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int s = k * 32 + lane;
+            if ((C.lm[k] >> lane) & 1u) S.vsd[s] = sd[k];
+            if ((om[k] >> lane) & 1u) S.fl[base + before + __popc(om[k] & ((1u << lane) - 1u))] = (uint8_t)s;
+            before += __popc(om[k]);
+        }
+        __syncwarp();
+        const bool edge = lane < 3 * R;
+        int x = 0, y = 0, a = 0, b = 0;
+        bool bnd = false, bad = false;
+        if (edge) {
+            const int xi = (lane * 11) >> 5;          // lane / 3 for lane < 32
+            const int e = lane - 3 * xi;
+            x = S.fl[base + xi];
+            const uint32_t xt_ = S.tri[x], xa_ = S.adj[x];
+            a = plane_of(xt_, e);
+            b = plane_of(xt_, e == 2 ? 0 : e + 1);
+            y = plane_of(xa_, e);
+            bad = a >= f || b >= f || y >= S_t::V;
+            bnd = !bad && !bit_k<K>(om, y);
+        }
+        if (__any_sync(FULL, bad)) return -ST_DEGEN;
+        const unsigned bm = __ballot_sync(FULL, bnd);
+        const int B = __popc(bm);
+        // capacity: the stack (with the pushed Outside slots) must hold B
+        if (B > base + R) return -ST_VCAP;
+        const int q = __popc(bm & ((1u << lane) - 1u));
+        int slot = 0;
+        uint32_t ty = 0;
+        T px = 0, py = 0, pz = 0, pe = 0;
+        if (bnd) {
+            if constexpr (GUARD) {
+                // the vertex of planes (a, b, f) by Cramer's rule (see above)
+                const T ax = S.px[a], ay = S.py[a], az = S.pz[a], ah = S.pd[a];
+                const T bx = S.px[b], by = S.py[b], bz = S.pz[b], bh = S.pd[b];
+                const T bfx = by * nz - bz * ny, bfy = bz * nx - bx * nz, bfz = bx * ny - by * nx;
+                const T fax = ny * az - nz * ay, fay = nz * ax - nx * az, faz = nx * ay - ny * ax;
+                const T abx = ay * bz - az * by, aby = az * bx - ax * bz, abz = ax * by - ay * bx;
+                const T det = ax * bfx + ay * bfy + az * bfz;
+                const T inv = (T)1 / det;
+                px = (ah * bfx + bh * fax + off * abx) * inv;
+                py = (ah * bfy + bh * fay + off * aby) * inv;
+                pz = (ah * bfz + bh * faz + off * abz) * inv;
+                const T dhat = fabs(det) / (S.pn[a] * S.pn[b] * rn);
+                pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) / max(dhat, (T)1e-30);
+                if (!(pe < (T)1e30)) pe = (T)1e30;
+            } else {
+                const T xx = S.vx[x], xy = S.vy[x], xz = S.vz[x], xsd = S.vsd[x];
+                const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
+                const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / (xsd - ysd);
+                px = xx + (yx - xx) * t;
+                py = xy + (yy - xy) * t;
+                pz = xz + (yz - xz) * t;
+            }
+            ty = S.tri[y];
+            slot = S.fl[base + R - 1 - q];
+        }
+        __syncwarp();
+        if (bnd) {
+            S.vx[slot] = px;
+            S.vy[slot] = py;
+            S.vz[slot] = pz;
+            if constexpr (GUARD) S.ve[slot] = pe;
+            S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
+            // Y's pointer back to X is the edge (b, a) of Y's triple.
+            const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
+                           : (plane_of(ty, 1) == b && plane_of(ty, 2) == a) ? 1
+                                                                            : 2;
+            reinterpret_cast<uint8_t*>(S.adj)[4 * y + yi] = (uint8_t)slot;
+            S.mapf[a] = (uint8_t)slot;
+            S.maps[b] = (uint8_t)slot;
+        }
+        __syncwarp();
+        if (bnd) {
+            // across (b, f): the new vertex whose first plane is b; across
+            // (f, a): the one whose second plane is a
+            const int n1 = S.mapf[b], n2 = S.maps[a];
+            bad = (S.mapf[a] != slot) || (S.maps[b] != slot) || n1 == 0xFF || n2 == 0xFF;
+            S.adj[slot] = (uint32_t)y | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
+        }
+        __syncwarp();
+        if (bnd) {
+            S.mapf[a] = 0xFF;
+            S.maps[b] = 0xFF;
+        }
+        if (__any_sync(FULL, bad)) return -ST_DEGEN;
+        C.nfree = base + R - B;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const uint32_t nm = __reduce_or_sync(FULL, (bnd && (slot >> 5) == k) ? (1u << (slot & 31)) : 0u);
+            C.lm[k] = (C.lm[k] & ~om[k]) | nm;
+            if ((nm >> lane) & 1u) {
+                const int s = k * 32 + lane;
+                C.vx[k] = S.vx[s];
+                C.vy[k] = S.vy[s];
+                C.vz[k] = S.vz[s];
+                if constexpr (GUARD) C.ve[k] = S.ve[s];
+            }
+        }
+        // the plane, one field per lane
+        if (lane < 7) {
+            if (lane == 0) S.px[f] = nx;
+            else if (lane == 1) S.py[f] = ny;
+            else if (lane == 2) S.pz[f] = nz;
+            else if (lane == 3) S.pd[f] = off;
+            else if (lane == 4) S.pn[f] = rn;
+            else if (lane == 5) S.pid[f] = id;
+            else S.psrc[f] = src;
+        }
+        C.np = f + 1;
+        __syncwarp();
+        return B + 1;
+    }
 
     // Signed distances of live vertices go to shared memory for the lanes
     // that place new vertices; my Outside vertices' triples and neighbours are
@@ -424,6 +550,23 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         S.psrc[f] = src;
     }
     C.np = f + 1;
+    // rebuild the free-slot stack from the live masks
+    {
+        int n = 0;
+#pragma unroll
+        for (int k = K - 1; k >= 0; --k) {
+            uint32_t fr = ~C.lm[k];
+            if (K == 8 && k == K - 1) fr &= 0x7FFFFFFFu;
+            const int c = __popc(fr);
+            // descending slot order, so the lowest free slot is on top
+            if ((fr >> (31 - lane)) & 1u) {
+                const uint32_t above = lane == 0 ? 0u : (fr >> (32 - lane));
+                S.fl[n + __popc(above)] = (uint8_t)(k * 32 + 31 - lane);
+            }
+            n += c;
+        }
+        C.nfree = n;
+    }
     __syncwarp();
     return B + 1;
 }
@@ -566,6 +709,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         S.mapf[i] = 0xFF;
         S.maps[i] = 0xFF;
     }
+    // free-slot stack: slots 8 .. VUSE-1, lowest on top
+    C.nfree = S_t::VUSE - 8;
+    for (int i = lane; i < C.nfree; i += 32) S.fl[i] = (uint8_t)(S_t::VUSE - 1 - i);
     __syncwarp();
     T R2 = live_r2(C, lane);
     // cR: bound on the FP32 rounding of one plane test, relative to the cell radius
