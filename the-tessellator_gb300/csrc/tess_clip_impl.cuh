@@ -197,161 +197,14 @@ struct CellRegs {
     int nfree;        // entries on the free-slot stack (warp-uniform)
 };
 
-// Clip the cell by the half-space {x : n.x - off <= 0}.
-//   FP64 form: n is the unit normal of the bisector and off its offset; a
-//     vertex is Outside when n.v - off > 1e-12 (vector3.rs:170-193,
-//     polyhedron.rs:221).
-//   FP32 form: n = r and off = r.r / 2 (the same plane, scaled by rn = |r|).
-//     Every vertex carries a bound e_v on its position error.  A test with
-//     |n.v - off| <= rn * (e_v + cR), cR bounding the plane's own rounding,
-//     cannot be decided in FP32: the cell goes to the FP64 form (ST_GUARD).
-// Returns 1 when vertices were cut off, 0 when nothing was Outside, or
-// -status.
+// The general form of a cut (more than 32 edges leave the Outside
+// vertices): owners loop over their edges; placement runs in rounds of 32.
+// Kept out of line: it is rare and its code would crowd the hot loop.
 template <typename T, int K, bool GUARD>
-__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T rn, T cR, int32_t id,
-                   uint32_t src, int lane) {
+__device__ __noinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, const T (&sd)[K],
+                                        const uint32_t (&om)[K], T nx, T ny, T nz, T off, T rn, T cR,
+                                        int32_t id, uint32_t src, int lane) {
     using S_t = Smem<T, K>;
-    T sd[K];
-    uint32_t om[K];
-    bool gh = false;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const bool live = (C.lm[k] >> lane) & 1u;
-        sd[k] = sdist(nx, ny, nz, off, C.vx[k], C.vy[k], C.vz[k]);
-        const bool out = live && sd[k] > (GUARD ? (T)0 : (T)kTolerance);
-        if constexpr (GUARD) gh |= live && fabs(sd[k]) <= rn * (C.ve[k] + cR);
-        om[k] = __ballot_sync(FULL, out);
-    }
-    if (GUARD && __any_sync(FULL, gh)) return -ST_GUARD;
-    uint32_t anyo = 0;
-#pragma unroll
-    for (int k = 0; k < K; ++k) anyo |= om[k];
-    if (!anyo) return 0;
-    if (C.np >= S_t::P) return -ST_PCAP;
-    int R = 0;
-#pragma unroll
-    for (int k = 0; k < K; ++k) R += __popc(om[k]);
-    if (3 * R <= 32) {
-        // Fast path: one lane per edge of an Outside vertex.  The Outside
-        // slots are pushed onto the free-slot stack; the new vertices pop
-        // slots from its top (reusing freed slots first).
-        const int f = C.np;
-        const int base = C.nfree;
-        int before = 0;
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const int s = k * 32 + lane;
-            if ((C.lm[k] >> lane) & 1u) S.vsd[s] = sd[k];
-            if ((om[k] >> lane) & 1u) S.fl[base + before + __popc(om[k] & ((1u << lane) - 1u))] = (uint8_t)s;
-            before += __popc(om[k]);
-        }
-        __syncwarp();
-        const bool edge = lane < 3 * R;
-        int x = 0, y = 0, a = 0, b = 0;
-        bool bnd = false, bad = false;
-        if (edge) {
-            const int xi = (lane * 11) >> 5;          // lane / 3 for lane < 32
-            const int e = lane - 3 * xi;
-            x = S.fl[base + xi];
-            const uint32_t xt_ = S.tri[x], xa_ = S.adj[x];
-            a = plane_of(xt_, e);
-            b = plane_of(xt_, e == 2 ? 0 : e + 1);
-            y = plane_of(xa_, e);
-            bad = a >= f || b >= f || y >= S_t::V;
-            bnd = !bad && !bit_k<K>(om, y);
-        }
-        if (__any_sync(FULL, bad)) return -ST_DEGEN;
-        const unsigned bm = __ballot_sync(FULL, bnd);
-        const int B = __popc(bm);
-        // capacity: the stack (with the pushed Outside slots) must hold B
-        if (B > base + R) return -ST_VCAP;
-        const int q = __popc(bm & ((1u << lane) - 1u));
-        int slot = 0;
-        uint32_t ty = 0;
-        T px = 0, py = 0, pz = 0, pe = 0;
-        if (bnd) {
-            if constexpr (GUARD) {
-                // the vertex of planes (a, b, f) by Cramer's rule (see above)
-                const T ax = S.px[a], ay = S.py[a], az = S.pz[a], ah = S.pd[a];
-                const T bx = S.px[b], by = S.py[b], bz = S.pz[b], bh = S.pd[b];
-                const T bfx = by * nz - bz * ny, bfy = bz * nx - bx * nz, bfz = bx * ny - by * nx;
-                const T fax = ny * az - nz * ay, fay = nz * ax - nx * az, faz = nx * ay - ny * ax;
-                const T abx = ay * bz - az * by, aby = az * bx - ax * bz, abz = ax * by - ay * bx;
-                const T det = ax * bfx + ay * bfy + az * bfz;
-                const T inv = (T)1 / det;
-                px = (ah * bfx + bh * fax + off * abx) * inv;
-                py = (ah * bfy + bh * fay + off * aby) * inv;
-                pz = (ah * bfz + bh * faz + off * abz) * inv;
-                const T dhat = fabs(det) / (S.pn[a] * S.pn[b] * rn);
-                pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) / max(dhat, (T)1e-30);
-                if (!(pe < (T)1e30)) pe = (T)1e30;
-            } else {
-                const T xx = S.vx[x], xy = S.vy[x], xz = S.vz[x], xsd = S.vsd[x];
-                const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
-                const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / (xsd - ysd);
-                px = xx + (yx - xx) * t;
-                py = xy + (yy - xy) * t;
-                pz = xz + (yz - xz) * t;
-            }
-            ty = S.tri[y];
-            slot = S.fl[base + R - 1 - q];
-        }
-        __syncwarp();
-        if (bnd) {
-            S.vx[slot] = px;
-            S.vy[slot] = py;
-            S.vz[slot] = pz;
-            if constexpr (GUARD) S.ve[slot] = pe;
-            S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
-            // Y's pointer back to X is the edge (b, a) of Y's triple.
-            const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
-                           : (plane_of(ty, 1) == b && plane_of(ty, 2) == a) ? 1
-                                                                            : 2;
-            reinterpret_cast<uint8_t*>(S.adj)[4 * y + yi] = (uint8_t)slot;
-            S.mapf[a] = (uint8_t)slot;
-            S.maps[b] = (uint8_t)slot;
-        }
-        __syncwarp();
-        if (bnd) {
-            // across (b, f): the new vertex whose first plane is b; across
-            // (f, a): the one whose second plane is a
-            const int n1 = S.mapf[b], n2 = S.maps[a];
-            bad = (S.mapf[a] != slot) || (S.maps[b] != slot) || n1 == 0xFF || n2 == 0xFF;
-            S.adj[slot] = (uint32_t)y | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
-        }
-        __syncwarp();
-        if (bnd) {
-            S.mapf[a] = 0xFF;
-            S.maps[b] = 0xFF;
-        }
-        if (__any_sync(FULL, bad)) return -ST_DEGEN;
-        C.nfree = base + R - B;
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const uint32_t nm = __reduce_or_sync(FULL, (bnd && (slot >> 5) == k) ? (1u << (slot & 31)) : 0u);
-            C.lm[k] = (C.lm[k] & ~om[k]) | nm;
-            if ((nm >> lane) & 1u) {
-                const int s = k * 32 + lane;
-                C.vx[k] = S.vx[s];
-                C.vy[k] = S.vy[s];
-                C.vz[k] = S.vz[s];
-                if constexpr (GUARD) C.ve[k] = S.ve[s];
-            }
-        }
-        // the plane, one field per lane
-        if (lane < 7) {
-            if (lane == 0) S.px[f] = nx;
-            else if (lane == 1) S.py[f] = ny;
-            else if (lane == 2) S.pz[f] = nz;
-            else if (lane == 3) S.pd[f] = off;
-            else if (lane == 4) S.pn[f] = rn;
-            else if (lane == 5) S.pid[f] = id;
-            else S.psrc[f] = src;
-        }
-        C.np = f + 1;
-        __syncwarp();
-        return B + 1;
-    }
 
     // Signed distances of live vertices go to shared memory for the lanes
     // that place new vertices; my Outside vertices' triples and neighbours are
@@ -569,6 +422,164 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
     }
     __syncwarp();
     return B + 1;
+}
+
+// Clip the cell by the half-space {x : n.x - off <= 0}.
+//   FP64 form: n is the unit normal of the bisector and off its offset; a
+//     vertex is Outside when n.v - off > 1e-12 (vector3.rs:170-193,
+//     polyhedron.rs:221).
+//   FP32 form: n = r and off = r.r / 2 (the same plane, scaled by rn = |r|).
+//     Every vertex carries a bound e_v on its position error.  A test with
+//     |n.v - off| <= rn * (e_v + cR), cR bounding the plane's own rounding,
+//     cannot be decided in FP32: the cell goes to the FP64 form (ST_GUARD).
+// Returns 1 when vertices were cut off, 0 when nothing was Outside, or
+// -status.
+template <typename T, int K, bool GUARD>
+__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T rn, T cR, int32_t id,
+                   uint32_t src, int lane) {
+    using S_t = Smem<T, K>;
+    T sd[K];
+    uint32_t om[K];
+    bool gh = false;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const bool live = (C.lm[k] >> lane) & 1u;
+        sd[k] = sdist(nx, ny, nz, off, C.vx[k], C.vy[k], C.vz[k]);
+        const bool out = live && sd[k] > (GUARD ? (T)0 : (T)kTolerance);
+        if constexpr (GUARD) gh |= live && fabs(sd[k]) <= rn * (C.ve[k] + cR);
+        om[k] = __ballot_sync(FULL, out);
+    }
+    if (GUARD && __any_sync(FULL, gh)) return -ST_GUARD;
+    uint32_t anyo = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) anyo |= om[k];
+    if (!anyo) return 0;
+    if (C.np >= S_t::P) return -ST_PCAP;
+    int R = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) R += __popc(om[k]);
+    if (3 * R <= 32) {
+        // Fast path: one lane per edge of an Outside vertex.  The Outside
+        // slots are pushed onto the free-slot stack; the new vertices pop
+        // slots from its top (reusing freed slots first).
+        const int f = C.np;
+        const int base = C.nfree;
+        int before = 0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int s = k * 32 + lane;
+            if ((C.lm[k] >> lane) & 1u) S.vsd[s] = sd[k];
+            if ((om[k] >> lane) & 1u) S.fl[base + before + __popc(om[k] & ((1u << lane) - 1u))] = (uint8_t)s;
+            before += __popc(om[k]);
+        }
+        __syncwarp();
+        const bool edge = lane < 3 * R;
+        int x = 0, y = 0, a = 0, b = 0;
+        bool bnd = false, bad = false;
+        if (edge) {
+            const int xi = (lane * 11) >> 5;          // lane / 3 for lane < 32
+            const int e = lane - 3 * xi;
+            x = S.fl[base + xi];
+            const uint32_t xt_ = S.tri[x], xa_ = S.adj[x];
+            a = plane_of(xt_, e);
+            b = plane_of(xt_, e == 2 ? 0 : e + 1);
+            y = plane_of(xa_, e);
+            bad = a >= f || b >= f || y >= S_t::V;
+            bnd = !bad && !bit_k<K>(om, y);
+        }
+        if (__any_sync(FULL, bad)) return -ST_DEGEN;
+        const unsigned bm = __ballot_sync(FULL, bnd);
+        const int B = __popc(bm);
+        // capacity: the stack (with the pushed Outside slots) must hold B
+        if (B > base + R) return -ST_VCAP;
+        const int q = __popc(bm & ((1u << lane) - 1u));
+        int slot = 0;
+        uint32_t ty = 0;
+        T px = 0, py = 0, pz = 0, pe = 0;
+        if (bnd) {
+            if constexpr (GUARD) {
+                // the vertex of planes (a, b, f) by Cramer's rule (see above)
+                const T ax = S.px[a], ay = S.py[a], az = S.pz[a], ah = S.pd[a];
+                const T bx = S.px[b], by = S.py[b], bz = S.pz[b], bh = S.pd[b];
+                const T bfx = by * nz - bz * ny, bfy = bz * nx - bx * nz, bfz = bx * ny - by * nx;
+                const T fax = ny * az - nz * ay, fay = nz * ax - nx * az, faz = nx * ay - ny * ax;
+                const T abx = ay * bz - az * by, aby = az * bx - ax * bz, abz = ax * by - ay * bx;
+                const T det = ax * bfx + ay * bfy + az * bfz;
+                const T inv = (T)1 / det;
+                px = (ah * bfx + bh * fax + off * abx) * inv;
+                py = (ah * bfy + bh * fay + off * aby) * inv;
+                pz = (ah * bfz + bh * faz + off * abz) * inv;
+                const T dhat = fabs(det) / (S.pn[a] * S.pn[b] * rn);
+                pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) / max(dhat, (T)1e-30);
+                if (!(pe < (T)1e30)) pe = (T)1e30;
+            } else {
+                const T xx = S.vx[x], xy = S.vy[x], xz = S.vz[x], xsd = S.vsd[x];
+                const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
+                const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / (xsd - ysd);
+                px = xx + (yx - xx) * t;
+                py = xy + (yy - xy) * t;
+                pz = xz + (yz - xz) * t;
+            }
+            ty = S.tri[y];
+            slot = S.fl[base + R - 1 - q];
+        }
+        __syncwarp();
+        if (bnd) {
+            S.vx[slot] = px;
+            S.vy[slot] = py;
+            S.vz[slot] = pz;
+            if constexpr (GUARD) S.ve[slot] = pe;
+            S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
+            // Y's pointer back to X is the edge (b, a) of Y's triple.
+            const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
+                           : (plane_of(ty, 1) == b && plane_of(ty, 2) == a) ? 1
+                                                                            : 2;
+            reinterpret_cast<uint8_t*>(S.adj)[4 * y + yi] = (uint8_t)slot;
+            S.mapf[a] = (uint8_t)slot;
+            S.maps[b] = (uint8_t)slot;
+        }
+        __syncwarp();
+        if (bnd) {
+            // across (b, f): the new vertex whose first plane is b; across
+            // (f, a): the one whose second plane is a
+            const int n1 = S.mapf[b], n2 = S.maps[a];
+            bad = (S.mapf[a] != slot) || (S.maps[b] != slot) || n1 == 0xFF || n2 == 0xFF;
+            S.adj[slot] = (uint32_t)y | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
+        }
+        __syncwarp();
+        if (bnd) {
+            S.mapf[a] = 0xFF;
+            S.maps[b] = 0xFF;
+        }
+        if (__any_sync(FULL, bad)) return -ST_DEGEN;
+        C.nfree = base + R - B;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const uint32_t nm = __reduce_or_sync(FULL, (bnd && (slot >> 5) == k) ? (1u << (slot & 31)) : 0u);
+            C.lm[k] = (C.lm[k] & ~om[k]) | nm;
+            if ((nm >> lane) & 1u) {
+                const int s = k * 32 + lane;
+                C.vx[k] = S.vx[s];
+                C.vy[k] = S.vy[s];
+                C.vz[k] = S.vz[s];
+                if constexpr (GUARD) C.ve[k] = S.ve[s];
+            }
+        }
+        // the plane, one field per lane
+        if (lane < 7) {
+            if (lane == 0) S.px[f] = nx;
+            else if (lane == 1) S.py[f] = ny;
+            else if (lane == 2) S.pz[f] = nz;
+            else if (lane == 3) S.pd[f] = off;
+            else if (lane == 4) S.pn[f] = rn;
+            else if (lane == 5) S.pid[f] = id;
+            else S.psrc[f] = src;
+        }
+        C.np = f + 1;
+        __syncwarp();
+        return B + 1;
+    }
+    return cut_general<T, K, GUARD>(S, C, sd, om, nx, ny, nz, off, rn, cR, id, src, lane);
 }
 
 // Squared radius of the cell about its site: max |v|^2 over live vertices;
