@@ -200,11 +200,18 @@ struct CellRegs {
 // The general form of a cut (more than 32 edges leave the Outside
 // vertices): owners loop over their edges; placement runs in rounds of 32.
 // Kept out of line: it is rare and its code would crowd the hot loop.
+template <typename T, int K>
+struct Regs {
+    T v[K];
+};
+
 template <typename T, int K, bool GUARD>
-__device__ __noinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, const T (&sd)[K],
-                                        const uint32_t (&om)[K], T nx, T ny, T nz, T off, T rn, T cR,
+__device__ __noinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, const Regs<T, K> sdv,
+                                        const Regs<uint32_t, K> omv, T nx, T ny, T nz, T off, T rn, T cR,
                                         int32_t id, uint32_t src, int lane) {
     using S_t = Smem<T, K>;
+    const T(&sd)[K] = sdv.v;
+    const uint32_t(&om)[K] = omv.v;
 
     // Signed distances of live vertices go to shared memory for the lanes
     // that place new vertices; my Outside vertices' triples and neighbours are
@@ -579,7 +586,14 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         __syncwarp();
         return B + 1;
     }
-    return cut_general<T, K, GUARD>(S, C, sd, om, nx, ny, nz, off, rn, cR, id, src, lane);
+    Regs<T, K> sdv;
+    Regs<uint32_t, K> omv;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        sdv.v[k] = sd[k];
+        omv.v[k] = om[k];
+    }
+    return cut_general<T, K, GUARD>(S, C, sdv, omv, nx, ny, nz, off, rn, cR, id, src, lane);
 }
 
 // Squared radius of the cell about its site: max |v|^2 over live vertices;
@@ -735,6 +749,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     const int cby = axis_index(sy, D.glo[1], D.ghi[1], D.inv[1], cpd);
     const int cbz = axis_index(sz, D.glo[2], D.ghi[2], D.inv[2], cpd);
     const double radius = P.search_radius;
+    const bool has_radius = radius >= 0.0;
     const int64_t tgroup = P.target_group;
     const TabEntry* tab = P.table + D.tab_base;
 
@@ -849,7 +864,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         const int x = cbx + i, y = cby + j, z = cbz + k;
         if (x < 0 || x >= cpd || y < 0 || y >= cpd || z < 0 || z >= cpd) return -1;
         // no point of this bin can cut: it lies beyond twice the cell radius
-        if (near_ok && near2(i, j, k) * (1.0f - 1e-4f) >= (float)(4.0 * (double)R2))
+        if (near_ok && near2(i, j, k) * (1.0f - 1e-4f) >= round_up_f((T)4 * R2))
             return -1;
         return (long long)(bin_base + ((uint64_t)x * cpd + y) * cpd + z);
     };
@@ -876,7 +891,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             e.j = te.j;
             e.k = te.k;
             e.key = te.key;
-            if (radius >= 0.0 && gap_key(D.size, e.i, e.j, e.k) > radius) e.key = INFINITY;
+            if (has_radius && gap_key(D.size, e.i, e.j, e.k) > radius) e.key = INFINITY;
             const long long lb = bin_of(e.i, e.j, e.k);
             if (lb >= 0) {
                 e.beg = P.delims[lb];
@@ -901,8 +916,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         unsigned ba = ea.beg, ca = lane < na ? ea.cnt : 0u;
         unsigned bb = eb.beg, cb = lane < nb ? eb.cnt : 0u;
         // re-test the bins against the current (smaller) radius
-        if (ca && near_ok && near2(ea.i, ea.j, ea.k) * (1.0f - 1e-4f) >= (float)(4.0 * (double)R2)) ca = 0;
-        if (cb && near_ok && near2(eb.i, eb.j, eb.k) * (1.0f - 1e-4f) >= (float)(4.0 * (double)R2)) cb = 0;
+        const float lim4 = round_up_f((T)4 * R2);
+        if (ca && near_ok && near2(ea.i, ea.j, ea.k) * (1.0f - 1e-4f) >= lim4) ca = 0;
+        if (cb && near_ok && near2(eb.i, eb.j, eb.k) * (1.0f - 1e-4f) >= lim4) cb = 0;
         const bool last = (ma | mb) != 0;
         const uint32_t used = (uint32_t)(na + nb);
         t += used;
@@ -1266,8 +1282,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     }
 }
 
+// K = 2: 8 warps per block, two blocks per SM (registers capped at 128).
 template <typename T, int K, bool GEO>
-__global__ void k_clip(ClipParams P) {
+__global__ void __launch_bounds__(K == 2 ? 256 : 128, K == 2 ? 2 : 1) k_clip(ClipParams P) {
     extern __shared__ __align__(16) unsigned char smraw[];
     Smem<T, K>& S = reinterpret_cast<Smem<T, K>*>(smraw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
