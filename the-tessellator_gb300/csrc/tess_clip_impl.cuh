@@ -54,6 +54,9 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr float kVertexErr = 1.5e-6f;
 // Shell-table entries per walk batch: 32 (one per lane) or 64 (two per lane).
 constexpr bool kBatch2 = false;
+// Load the next batch's table entries and bin ranges before cutting the
+// current batch (overlaps their latency, costs registers).
+constexpr bool kPrefetch = true;
 
 template <typename T, int K>
 struct Smem {
@@ -199,14 +202,13 @@ struct CellRegs {
 
 // The general form of a cut (more than 32 edges leave the Outside
 // vertices): owners loop over their edges; placement runs in rounds of 32.
-// Kept out of line: it is rare and its code would crowd the hot loop.
 template <typename T, int K>
 struct Regs {
     T v[K];
 };
 
 template <typename T, int K, bool GUARD>
-__device__ __noinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, const Regs<T, K> sdv,
+__device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, const Regs<T, K> sdv,
                                         const Regs<uint32_t, K> omv, T nx, T ny, T nz, T off, T rn, T cR,
                                         int32_t id, uint32_t src, int lane) {
     using S_t = Smem<T, K>;
@@ -450,6 +452,12 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
     bool gh = false;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
+        sd[k] = (T)0;
+        om[k] = 0;
+        // register sets without live vertices are skipped (the free-slot
+        // stack hands out the lowest slots first, so the upper sets are
+        // usually empty)
+        if (C.lm[k] == 0) continue;
         const bool live = (C.lm[k] >> lane) & 1u;
         sd[k] = sdist(nx, ny, nz, off, C.vx[k], C.vy[k], C.vz[k]);
         const bool out = live && sd[k] > (GUARD ? (T)0 : (T)kTolerance);
@@ -603,6 +611,7 @@ __device__ __forceinline__ T live_r2(const CellRegs<T, K>& C, int lane) {
     T r2 = 0;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
+        if (C.lm[k] == 0) continue;
         if ((C.lm[k] >> lane) & 1u) {
             T q = C.vx[k] * C.vx[k] + C.vy[k] * C.vy[k] + C.vz[k] * C.vz[k];
             if (sizeof(T) == 4) {
@@ -922,13 +931,17 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         const bool last = (ma | mb) != 0;
         const uint32_t used = (uint32_t)(na + nb);
         t += used;
-        if (!last) {
+        if (kPrefetch && !last) {
             load_entry(t + lane, ea);
             if (kBatch2) load_entry(t + 32 + lane, eb);
         }
         ++W.batches;
         status = process(ba, ca, bb, cb);
         if (status != ST_OK) break;
+        if (!kPrefetch && !last) {
+            load_entry(t + lane, ea);
+            if (kBatch2) load_entry(t + 32 + lane, eb);
+        }
         if (last) {
             phase2 = (t >= tab_len) && isfinite(D.tab_kmax);
             break;
