@@ -75,6 +75,7 @@ struct Smem {
     uint32_t cbeg2[32], ccnt[32];     // second-half bins: starts and prefix counts
     uint16_t items[V + 32];           // boundary edges of a cut: slot | edge << 8
     uint8_t fl[V + 32];               // free-slot stack (top = lowest free slot)
+    uint32_t pused[(P + 31) / 32];    // plane recycling: planes referenced by live vertices
     int32_t flist[P];                 // finalize: compacted face ids
     uint8_t fsta[P];                  // finalize: one vertex of each face
     uint8_t mapf[P], maps[P];         // new-vertex ring maps
@@ -202,6 +203,38 @@ struct CellRegs {
 
 // The general form of a cut (more than 32 edges leave the Outside
 // vertices): owners loop over their edges; placement runs in rounds of 32.
+// The plane table is full: find a plane id (not a wall) that no live vertex
+// references any more, or -1.  Faces cut away entirely leave such ids
+// behind; cells cut hundreds of times (next to dense clusters) need them.
+template <typename T, int K>
+__device__ __noinline__ int recycle_plane(Smem<T, K>& S, const CellRegs<T, K>& C, int lane) {
+    using S_t = Smem<T, K>;
+    constexpr int NW = (S_t::P + 31) / 32;
+    for (int w = lane; w < NW; w += 32) S.pused[w] = 0;
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if ((C.lm[k] >> lane) & 1u) {
+            const uint32_t t = S.tri[k * 32 + lane];
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                const int p = plane_of(t, e);
+                if (p < S_t::P) atomicOr(&S.pused[p >> 5], 1u << (p & 31));
+            }
+        }
+    }
+    __syncwarp();
+    int res = -1;
+    for (int w = 0; w < NW && res < 0; ++w) {
+        uint32_t fr = ~S.pused[w];
+        if (w == 0) fr &= ~0x3Fu;                                  // the walls stay
+        if (w == NW - 1 && (S_t::P & 31)) fr &= (1u << (S_t::P & 31)) - 1u;
+        if (fr) res = w * 32 + __ffs(fr) - 1;
+    }
+    __syncwarp();
+    return res;
+}
+
 template <typename T, int K>
 struct Regs {
     T v[K];
@@ -210,7 +243,7 @@ struct Regs {
 template <typename T, int K, bool GUARD>
 __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, const Regs<T, K> sdv,
                                         const Regs<uint32_t, K> omv, T nx, T ny, T nz, T off, T rn, T cR,
-                                        int32_t id, uint32_t src, int lane) {
+                                        int32_t id, uint32_t src, int f, int lane) {
     using S_t = Smem<T, K>;
     const T(&sd)[K] = sdv.v;
     const uint32_t(&om)[K] = omv.v;
@@ -271,7 +304,6 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
     }
     if (K == 8) fm[K - 1] &= 0x7FFFFFFFu;
     if (nlive + B > S_t::VUSE) return -ST_VCAP;
-    const int f = C.np;
     const int rounds = (B + 31) >> 5;
     if (rounds > 1) {
         // More than 32 new vertices (a cut through a large cell): make sure
@@ -411,7 +443,7 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
         S.pid[f] = id;
         S.psrc[f] = src;
     }
-    C.np = f + 1;
+    if (f >= C.np) C.np = f + 1;
     // rebuild the free-slot stack from the live masks
     {
         int n = 0;
@@ -469,7 +501,11 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
 #pragma unroll
     for (int k = 0; k < K; ++k) anyo |= om[k];
     if (!anyo) return 0;
-    if (C.np >= S_t::P) return -ST_PCAP;
+    int f = C.np;
+    if (f >= S_t::P) {
+        f = recycle_plane<T, K>(S, C, lane);
+        if (f < 0) return -ST_PCAP;
+    }
     int R = 0;
 #pragma unroll
     for (int k = 0; k < K; ++k) R += __popc(om[k]);
@@ -477,7 +513,6 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         // Fast path: one lane per edge of an Outside vertex.  The Outside
         // slots are pushed onto the free-slot stack; the new vertices pop
         // slots from its top (reusing freed slots first).
-        const int f = C.np;
         const int base = C.nfree;
         int before = 0;
 #pragma unroll
@@ -499,7 +534,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             a = plane_of(xt_, e);
             b = plane_of(xt_, e == 2 ? 0 : e + 1);
             y = plane_of(xa_, e);
-            bad = a >= f || b >= f || y >= S_t::V;
+            bad = a >= C.np || b >= C.np || y >= S_t::V;
             bnd = !bad && !bit_k<K>(om, y);
         }
         if (__any_sync(FULL, bad)) return -ST_DEGEN;
@@ -590,7 +625,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             else if (lane == 5) S.pid[f] = id;
             else S.psrc[f] = src;
         }
-        C.np = f + 1;
+        if (f >= C.np) C.np = f + 1;
         __syncwarp();
         return B + 1;
     }
@@ -601,7 +636,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         sdv.v[k] = sd[k];
         omv.v[k] = om[k];
     }
-    return cut_general<T, K, GUARD>(S, C, sdv, omv, nx, ny, nz, off, rn, cR, id, src, lane);
+    return cut_general<T, K, GUARD>(S, C, sdv, omv, nx, ny, nz, off, rn, cR, id, src, f, lane);
 }
 
 // Squared radius of the cell about its site: max |v|^2 over live vertices;
