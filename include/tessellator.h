@@ -252,6 +252,22 @@ tess_status tess_batch_neighbors_csr(tess_batch* b, uint64_t* offs, int32_t* nbr
                                      size_t cap, size_t* total);
 tess_status tess_batch_destroy(tess_batch* b);
 
+/* ------------------------------------------------------------------------ */
+/* No-allocation CSR offsets                                                  */
+/* ------------------------------------------------------------------------ */
+/* No counterpart in the reference.  For callers that may not allocate device
+ * memory (a fixed device budget, an allocator that owns all device memory, or
+ * a path where an allocation's implicit synchronisation is not allowed):
+ * d_offs[0..n] = exclusive scan of d_counts[0..n) (per-cell face counts),
+ * d_offs[n] = total, both in device memory, enqueued on `stream`
+ * (cudaStream_t, NULL = the default stream).  It calls no allocator.  Its
+ * scratch is a 128 KiB device array inside the library, which every GPU that
+ * loads the library holds until exit; n may be at most 2^26
+ * (TESS_E_CAPACITY beyond).  The first call on a device looks up that array's
+ * address, so make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race. */
+tess_status tess_csr_offsets_noalloc(const uint32_t* d_counts, size_t n, uint64_t* d_offs, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -606,6 +606,17 @@ tess_status validate_box(const double* lo, const double* hi) {
 
 }  // namespace
 
+namespace tess {
+void set_error(const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+}  // namespace tess
+
 struct tess_diagram {
     Engine E;
     uint32_t n = 0;

@@ -206,4 +206,7 @@ cudaError_t launch_csr_gather(const uint32_t* nface, const uint64_t* fstart, con
                               double* area_out, cudaStream_t s);
 size_t csr_tmp_words(uint32_t n);
 
+// Sets the calling thread's last error message (printf format).
+void set_error(const char* fmt, ...);
+
 }  // namespace tess

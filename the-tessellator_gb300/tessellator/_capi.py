@@ -30,7 +30,7 @@ EXPORTS = (
     "tess_cell_face_vertices", "tess_cell_original_index", "tess_cell_compute",
     "tess_cell_compute_at", "tess_volumes", "tess_neighbors_csr", "tess_results_device",
     "tess_batch_create", "tess_batch_compute", "tess_batch_stats", "tess_batch_volumes",
-    "tess_batch_neighbors_csr", "tess_batch_destroy",
+    "tess_batch_neighbors_csr", "tess_batch_destroy", "tess_csr_offsets_noalloc",
 )
 
 
@@ -114,6 +114,7 @@ def lib():
         "tess_batch_volumes": (st, [vp, dp]),
         "tess_batch_neighbors_csr": (st, [vp, u64p, i32p, dp, C.c_size_t, szp]),
         "tess_batch_destroy": (st, [vp]),
+        "tess_csr_offsets_noalloc": (st, [vp, C.c_size_t, vp, vp]),
     }
     for name in EXPORTS:
         fn = getattr(L, name)
