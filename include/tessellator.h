@@ -228,6 +228,48 @@ tess_status tess_neighbors_csr(tess_diagram* d, uint64_t* offs, int32_t* nbr, do
 tess_status tess_results_device(tess_diagram* d, const double** volumes, const uint64_t** offs,
                                 const int32_t** nbr, const double** area, size_t* total);
 
+/* ---- fixed-radius queries on the bin grid ---- */
+/* Batched over nq queries.  Results come back as CSR: offs[nq+1] and out[total]
+ * (u32 bin ids or original point indices), in the reference's order for each
+ * query.  offs and *total are always written (offs may be NULL); out is written
+ * when it is non-NULL and total <= cap, else TESS_E_CAPACITY (call again with a
+ * larger buffer; the results are deterministic).  With on_device = 1 every
+ * array argument is a device pointer; otherwise host memory.  These need only
+ * the grid, not compute_all.  radius follows the reference's arithmetic for
+ * any value, NaN and negative included. */
+
+/* Celery::find_cells_in_radius (celery.rs:753-796) for query positions
+ * xyz[nq][3]: the bins (id = i*cpd^2 + j*cpd + k) of the box [q - r, q + r]
+ * clamped to the point bounds whose gap distance to q's bin is at most r
+ * (check_cell_in_range, celery.rs:708-748), in i, j, k order. */
+tess_status tess_find_cells_in_radius(tess_diagram* d, const double* xyz, size_t nq, double radius,
+                                      int on_device, uint64_t* offs, uint32_t* cells, size_t cap,
+                                      size_t* total);
+/* Celery::find_neighbors_in_cell_radius (celery.rs:802-818, real_radius = 0):
+ * every point of those bins; find_neighbors_in_real_radius (celery.rs:825-855,
+ * real_radius = 1): those at squared distance <= radius * radius.  Bin by bin,
+ * ascending index within a bin. */
+tess_status tess_find_neighbors_in_radius(tess_diagram* d, const double* xyz, size_t nq, double radius,
+                                          int real_radius, int on_device, uint64_t* offs, uint32_t* ids,
+                                          size_t cap, size_t* total);
+/* Cell::compute_neighbor_cloud (interface.rs:348-365) for the cells
+ * cells[ncells] (original indices; NULL = every cell, ncells = n): the points
+ * of the bins the expanding search from the cell's position reaches before
+ * the first search-order key above radius (expand_all_in_radius,
+ * celery.rs:1023-1075; the key is a squared gap distance compared with the
+ * unsquared radius), self included, in search order (ties by i, j, k),
+ * ascending index within a bin; only target_group's points when
+ * target_group >= 0.  TESS_E_LIMIT if the radius reaches more than 2^26 bin
+ * offsets. */
+tess_status tess_neighbor_cloud(tess_diagram* d, const uint32_t* cells, size_t ncells, double radius,
+                                int64_t target_group, int on_device, uint64_t* offs, uint32_t* ids,
+                                size_t cap, size_t* total);
+/* The same from positions xyz[nq][3] (a Cell made by get_cell_at_particle,
+ * interface.rs:211-232). */
+tess_status tess_neighbor_cloud_at(tess_diagram* d, const double* xyz, size_t nq, double radius,
+                                   int64_t target_group, int on_device, uint64_t* offs, uint32_t* ids,
+                                   size_t cap, size_t* total);
+
 /* ------------------------------------------------------------------------ */
 /* Batch: many independent diagrams, one persistent launch per pass,          */
 /* captured in a CUDA graph (no reference counterpart: the reference builds   */

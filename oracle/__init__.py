@@ -114,6 +114,17 @@ def lib():
         L.or_all_stats.argtypes = [C.c_void_p, C.POINTER(CellStats)]
         L.or_all_seconds.restype = C.c_double
         L.or_all_seconds.argtypes = [C.c_void_p]
+        u64p = C.POINTER(C.c_uint64)
+        L.or_check_cell_in_range.restype = C.c_int
+        L.or_check_cell_in_range.argtypes = [C.c_void_p, d3, C.c_double, C.c_int64, C.c_int64, C.c_int64]
+        L.or_find_cells_in_radius.restype = C.c_size_t
+        L.or_find_cells_in_radius.argtypes = [C.c_void_p, d3, C.c_size_t, C.c_double, u64p, u32p, C.c_size_t]
+        L.or_find_neighbors_in_radius.restype = C.c_size_t
+        L.or_find_neighbors_in_radius.argtypes = [C.c_void_p, d3, C.c_size_t, C.c_double, C.c_int, u64p, u32p,
+                                                  C.c_size_t]
+        L.or_neighbor_cloud.restype = C.c_size_t
+        L.or_neighbor_cloud.argtypes = [C.c_void_p, d3, C.c_size_t, C.c_double, C.c_int64, u64p, u32p,
+                                        C.c_size_t]
         _lib = L
     return _lib
 
@@ -316,3 +327,30 @@ class Diagram:
         secs = L.or_all_seconds(a)
         L.or_all_destroy(a)
         return vol, offs, ids[:tot], areas[:tot], st, secs
+
+    # ---- radius queries (celery.rs:682-855, interface.rs:348-365) ----------
+    def check_cell_in_range(self, p, radius, i, j, k) -> bool:
+        p = _v(p)
+        return bool(lib().or_check_cell_in_range(self._h, _dp(p), radius, i, j, k))
+
+    def _csr_query(self, fn, q, *args):
+        q = _v(q).reshape(-1, 3)
+        nq = len(q)
+        offs = np.zeros(nq + 1, dtype=np.uint64)
+        u64 = C.POINTER(C.c_uint64)
+        total = fn(self._h, _dp(q), nq, *args, offs.ctypes.data_as(u64), None, 0)
+        out = np.zeros(max(total, 1), dtype=np.uint32)
+        fn(self._h, _dp(q), nq, *args, offs.ctypes.data_as(u64), _u32p(out), total)
+        return offs, out[:total]
+
+    def find_cells_in_radius(self, q, radius):
+        """(offsets, bin ids) for each query position."""
+        return self._csr_query(lib().or_find_cells_in_radius, q, radius)
+
+    def find_neighbors_in_radius(self, q, radius, real_radius: bool):
+        """(offsets, original indices): find_neighbors_in_{cell,real}_radius."""
+        return self._csr_query(lib().or_find_neighbors_in_radius, q, radius, 1 if real_radius else 0)
+
+    def neighbor_cloud(self, q, radius, target_group=-1):
+        """(offsets, original indices): compute_neighbor_cloud from each position."""
+        return self._csr_query(lib().or_neighbor_cloud, q, radius, target_group)

@@ -907,3 +907,151 @@ void or_all_results(const or_all* a, double* volumes, int64_t* offs, int64_t* id
 }
 void or_all_stats(const or_all* a, or_cell_stats* total) { *total = a->total; }
 double or_all_seconds(const or_all* a) { return a->seconds; }
+
+/* ------------------------------------------------------------------------ */
+/* radius queries (celery.rs:682-855, celery.rs:1023-1075, interface.rs:348-365) */
+/* ------------------------------------------------------------------------ */
+
+/* min_float / max_float, celery.rs:682-698: on ties and NaN the second
+ * argument wins. */
+static double rq_min(double a, double b) { return a < b ? a : b; }
+static double rq_max(double a, double b) { return a > b ? a : b; }
+
+static int64_t rq_gap(int64_t coord, int64_t index) {
+    int64_t v = coord - index;
+    if (v < 0) v = -v;
+    v -= 1;
+    return v < 0 ? 0 : v;
+}
+
+/* check_cell_in_range, celery.rs:708-748: the gap distance between the bin of
+ * p and bin (i, j, k), squared, against radius * radius. */
+int or_check_cell_in_range(const or_diagram* d, const double p[3], double radius, int64_t i, int64_t j,
+                           int64_t k) {
+    const or_grid_info* g = &d->g;
+    int64_t xi = or_axis_index(p[0], g->xmin, g->xmax, g->ix, g->cpd);
+    int64_t yi = or_axis_index(p[1], g->ymin, g->ymax, g->iy, g->cpd);
+    int64_t zi = or_axis_index(p[2], g->zmin, g->zmax, g->iz, g->cpd);
+    double a = (double)rq_gap(xi, i) * g->sx;
+    double b = (double)rq_gap(yi, j) * g->sy;
+    double c = (double)rq_gap(zi, k) * g->sz;
+    double ds = a * a + b * b + c * c;
+    return ds <= radius * radius;
+}
+
+/* find_cells_in_radius, celery.rs:753-796, for one position, in the
+ * reference's i, j, k loop order: with m, counts the bins into *m and stores
+ * them in out[*m..] as far as cap allows; with bins_tmp, collects them there. */
+static void rq_cells(const or_diagram* d, const double p[3], double radius, uint32_t* out, size_t cap,
+                     size_t* m, uint32_t** bins_tmp, size_t* bins_cap, size_t* nbins) {
+    const or_grid_info* g = &d->g;
+    double lx = rq_max(p[0] - radius, g->xmin), ly = rq_max(p[1] - radius, g->ymin);
+    double lz = rq_max(p[2] - radius, g->zmin);
+    double hx = rq_min(p[0] + radius, g->xmax), hy = rq_min(p[1] + radius, g->ymax);
+    double hz = rq_min(p[2] + radius, g->zmax);
+    int64_t i0 = or_axis_index(lx, g->xmin, g->xmax, g->ix, g->cpd);
+    int64_t j0 = or_axis_index(ly, g->ymin, g->ymax, g->iy, g->cpd);
+    int64_t k0 = or_axis_index(lz, g->zmin, g->zmax, g->iz, g->cpd);
+    int64_t i1 = or_axis_index(hx, g->xmin, g->xmax, g->ix, g->cpd);
+    int64_t j1 = or_axis_index(hy, g->ymin, g->ymax, g->iy, g->cpd);
+    int64_t k1 = or_axis_index(hz, g->zmin, g->zmax, g->iz, g->cpd);
+    *nbins = 0;
+    for (int64_t i = i0; i <= i1; ++i)
+        for (int64_t j = j0; j <= j1; ++j)
+            for (int64_t k = k0; k <= k1; ++k) {
+                if (!or_check_cell_in_range(d, p, radius, i, j, k)) continue;
+                uint32_t b = (uint32_t)((i * g->cpd + j) * g->cpd + k);   /* celery.rs:317-325 */
+                if (m) {
+                    if (out && *m < cap) out[*m] = b;
+                    ++*m;
+                }
+                if (bins_tmp) {
+                    if (*nbins == *bins_cap) {
+                        *bins_cap = *bins_cap ? 2 * *bins_cap : 64;
+                        *bins_tmp = (uint32_t*)realloc(*bins_tmp, *bins_cap * sizeof(uint32_t));
+                    }
+                    (*bins_tmp)[(*nbins)++] = b;
+                }
+            }
+}
+
+size_t or_find_cells_in_radius(const or_diagram* d, const double* q, size_t nq, double radius, uint64_t* offs,
+                               uint32_t* out, size_t cap) {
+    size_t m = 0;
+    for (size_t t = 0; t < nq; ++t) {
+        if (offs) offs[t] = m;
+        size_t nb = 0;
+        rq_cells(d, q + 3 * t, radius, out, cap, &m, NULL, NULL, &nb);
+    }
+    if (offs) offs[nq] = m;
+    return m;
+}
+
+/* distance_squared, celery.rs:700-702 */
+static double rq_dist2(const double a[3], const double b[3]) {
+    return (a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]);
+}
+
+/* find_neighbors_in_cell_radius (celery.rs:802-818, real_radius = 0) and
+ * find_neighbors_in_real_radius (celery.rs:825-855, real_radius = 1): the
+ * points of the bins find_cells_in_radius returns, in bin order and
+ * sorted_indices order within a bin; the real form keeps a point if its
+ * squared distance is at most radius * radius. */
+size_t or_find_neighbors_in_radius(const or_diagram* d, const double* q, size_t nq, double radius, int real_radius,
+                                   uint64_t* offs, uint32_t* out, size_t cap) {
+    size_t m = 0, bcap = 0, nb = 0;
+    uint32_t* bins = NULL;
+    const double r2 = radius * radius;
+    for (size_t t = 0; t < nq; ++t) {
+        if (offs) offs[t] = m;
+        rq_cells(d, q + 3 * t, radius, NULL, 0, NULL, &bins, &bcap, &nb);
+        for (size_t u = 0; u < nb; ++u)
+            for (uint32_t s = d->delims[bins[u]]; s < d->delims[bins[u] + 1]; ++s) {
+                uint32_t pi = d->sorted[s];
+                if (real_radius && !(rq_dist2(q + 3 * t, d->xyz + 3 * (size_t)pi) <= r2)) continue;
+                if (out && m < cap) out[m] = pi;
+                ++m;
+            }
+    }
+    if (offs) offs[nq] = m;
+    free(bins);
+    return m;
+}
+
+/* Cell::compute_neighbor_cloud, interface.rs:348-365: an ExpandingSearch
+ * from the cell's position (celery.rs:882-902) walked by
+ * expand_all_in_radius (celery.rs:1023-1075) over the whole search order
+ * (every offset up to cpd - 1 per axis, sorted by key; ties by i, j, k), which
+ * stops at the first key above the radius (a squared gap distance compared
+ * with the unsquared radius); out-of-grid bins are skipped; then the points
+ * of other groups are dropped when target_group >= 0. */
+size_t or_neighbor_cloud(const or_diagram* d, const double* q, size_t nq, double radius, int64_t target_group,
+                         uint64_t* offs, uint32_t* out, size_t cap) {
+    const or_grid_info* g = &d->g;
+    size_t ne = 0;
+    so_entry* e = build_order(g, (int32_t)(g->cpd - 1), -1.0, &ne);
+    size_t m = 0;
+    const int64_t c = g->cpd;
+    for (size_t t = 0; t < nq; ++t) {
+        if (offs) offs[t] = m;
+        const double* p = q + 3 * t;
+        int64_t bx = or_axis_index(p[0], g->xmin, g->xmax, g->ix, c);
+        int64_t by = or_axis_index(p[1], g->ymin, g->ymax, g->iy, c);
+        int64_t bz = or_axis_index(p[2], g->zmin, g->zmax, g->iz, c);
+        for (size_t u = 0; u < ne; ++u) {
+            if (e[u].key > radius) break;                           /* celery.rs:1037-1039 */
+            int64_t x = bx + e[u].i, y = by + e[u].j, z = bz + e[u].k;
+            if (x < 0 || x >= c || y < 0 || y >= c || z < 0 || z >= c) continue;
+            uint64_t b = (uint64_t)((x * c + y) * c + z);
+            for (uint32_t s = d->delims[b]; s < d->delims[b + 1]; ++s) {
+                uint32_t pi = d->sorted[s];
+                if (target_group >= 0 && (int64_t)d->groups[pi] != target_group) continue;
+                if (out && m < cap) out[m] = pi;
+                ++m;
+            }
+        }
+    }
+    if (offs) offs[nq] = m;
+    free(e);
+    return m;
+}

@@ -134,6 +134,19 @@ void or_all_results(const or_all* a, double* volumes, int64_t* offs, int64_t* id
 void or_all_stats(const or_all* a, or_cell_stats* total);
 double or_all_seconds(const or_all* a);
 
+/* ---- radius queries (celery.rs:682-855, interface.rs:348-365) ----
+ * Batched over nq query positions q (AoS).  Each returns the total number of
+ * results; offs (nq + 1 entries, nullable) gets CSR offsets and out the
+ * results, as far as they fit in cap.  Point results are original indices. */
+int or_check_cell_in_range(const or_diagram* d, const double p[3], double radius, int64_t i, int64_t j,
+                           int64_t k);                                                /* celery.rs:708-748 */
+size_t or_find_cells_in_radius(const or_diagram* d, const double* q, size_t nq, double radius, uint64_t* offs,
+                               uint32_t* out, size_t cap);                            /* celery.rs:753-796 */
+size_t or_find_neighbors_in_radius(const or_diagram* d, const double* q, size_t nq, double radius, int real_radius,
+                                   uint64_t* offs, uint32_t* out, size_t cap);        /* celery.rs:802-855 */
+size_t or_neighbor_cloud(const or_diagram* d, const double* q, size_t nq, double radius, int64_t target_group,
+                         uint64_t* offs, uint32_t* out, size_t cap);                  /* interface.rs:348-365 */
+
 #ifdef __cplusplus
 }
 #endif

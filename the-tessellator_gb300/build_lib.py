@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "tessellator", "libtessgpu.so")
 BUILD = os.path.join(ROOT, "_build", "tessgpu")
 SOURCES = ["tess_grid.cu", "tess_clip.cu", "tess_clip_f32.cu", "tess_clip_f64.cu", "tess_api.cu",
-           "tess_noalloc.cu"]
+           "tess_noalloc.cu", "tess_radius.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -47,7 +47,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return OUT
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
-    common = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+    # Host code keeps IEEE operation order (no FMA contraction on any host ISA):
+    # the radius table's keys must match the FP64 key formula bit for bit.
+    common = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                      "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
     def compile_one(src):

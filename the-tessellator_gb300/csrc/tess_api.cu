@@ -122,6 +122,27 @@ struct Engine {
     uint64_t* d_csr_tmp = nullptr;
     GeoOut* d_geo = nullptr;
     uint32_t* d_one = nullptr;
+    // radius queries: query positions / cells, per-query counts and offsets,
+    // scan scratch, results, and the search-order prefix of the last radius
+    double* d_rq = nullptr;
+    size_t rq_cap = 0;
+    uint32_t* d_rcell = nullptr;
+    size_t rcell_cap = 0;
+    uint32_t* d_rcnt = nullptr;
+    size_t rcnt_cap = 0;
+    uint64_t* d_roffs = nullptr;
+    size_t roffs_cap = 0;
+    uint64_t* d_rtmp = nullptr;
+    size_t rtmp_cap = 0;
+    uint32_t* d_rout = nullptr;
+    size_t rout_cap = 0;
+    short4* d_rtab = nullptr;
+    size_t rtab_cap = 0;
+    uint32_t rtab_len = 0;
+    bool rtab_valid = false;
+    uint64_t rtab_radius_bits = 0;
+    int* d_rerr = nullptr;
+    int sm_count = 0;
     // state
     bool built = false;
     bool computed = false;
@@ -149,6 +170,8 @@ struct Engine {
         for (auto& l : d_list) dfree(l);
         dfree(d_counters); dfree(d_work); dfree(d_offs); dfree(d_cnbr); dfree(d_carea); dfree(d_csr_tmp);
         dfree(d_geo); dfree(d_one);
+        dfree(d_rq); dfree(d_rcell); dfree(d_rcnt); dfree(d_roffs); dfree(d_rtmp); dfree(d_rout); dfree(d_rtab);
+        dfree(d_rerr);
         if (own_stream && stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -352,6 +375,7 @@ tess_status engine_build(Engine& E, bool check) {
     E.built = true;
     E.computed = false;
     E.csr_valid = false;
+    E.rtab_valid = false;
     return TESS_OK;
 }
 
@@ -595,6 +619,143 @@ tess_status engine_geo(Engine& E, int precision, uint32_t gs, const double* poin
         if (prec == TESS_PRECISION_FP64) break;
     }
     return fail(TESS_E_OVERFLOW, "cell could not be computed (status %d)", out->status);
+}
+
+// Device buffer of at least `need` elements (contents not kept).
+template <typename T>
+tess_status ensure(T** p, size_t& cap, size_t need) {
+    if (*p && need <= cap) return TESS_OK;
+    dfree(*p);
+    const size_t c = std::max(need, cap + cap / 2);
+    TRY(dalloc(p, c));
+    cap = c;
+    return TESS_OK;
+}
+
+// Largest search-order prefix a neighbour-cloud call may enumerate.
+constexpr size_t kMaxRadiusTable = (size_t)1 << 26;
+
+// Fixed-radius queries (tess_radius.cu) over nq queries: positions qxyz, or
+// cells (cloud only; null = every cell).  Count pass, scan, then the fill
+// pass into `out` when it is given and the total fits in `cap`.  With
+// on_device, qxyz / cells / offs / out are device pointers.
+tess_status engine_radius(Engine& E, int mode, bool by_cell, const double* qxyz, const uint32_t* cells, size_t nq,
+                          double radius, int64_t group, int on_device, uint64_t* offs, uint32_t* out, size_t cap,
+                          size_t* total) {
+    if (!E.built) return fail(TESS_E_STATE, "the diagram has no grid");
+    if (nq >= 0xFFFFFFFFull) return fail(TESS_E_INVALID, "too many queries (%zu)", nq);
+    if (nq && !by_cell && !qxyz) return fail(TESS_E_INVALID, "query positions are NULL");
+    CU(cudaSetDevice(E.device));
+    if (!E.sm_count) CU(cudaDeviceGetAttribute(&E.sm_count, cudaDevAttrMultiProcessorCount, E.device));
+    if (!E.d_rerr) TRY(dalloc(&E.d_rerr, 1));
+    RadiusParams p{};
+    p.desc = E.d_desc;
+    p.delims = E.d_delims;
+    p.sorted = E.d_sorted;
+    p.spx = E.d_spx;
+    p.spy = E.d_spy;
+    p.spz = E.d_spz;
+    p.sgroup = E.d_sgroup;
+    p.xyz = E.d_xyz;
+    p.inv = E.d_inv;
+    p.nq = (uint32_t)nq;
+    p.radius = radius;
+    p.group = group;
+    p.err = E.d_rerr;
+    if (!by_cell) {
+        if (on_device) {
+            p.qxyz = qxyz;
+        } else if (nq) {
+            TRY(ensure(&E.d_rq, E.rq_cap, 3 * nq));
+            CU(cudaMemcpyAsync(E.d_rq, qxyz, sizeof(double) * 3 * nq, cudaMemcpyHostToDevice, E.stream));
+            p.qxyz = E.d_rq;
+        }
+    } else if (cells) {
+        if (on_device) {
+            p.qcell = cells;
+        } else if (nq) {
+            for (size_t t = 0; t < nq; ++t)
+                if (cells[t] >= E.total)
+                    return fail(TESS_E_INVALID, "cell index %u out of range (n = %u)", cells[t], E.total);
+            TRY(ensure(&E.d_rcell, E.rcell_cap, nq));
+            CU(cudaMemcpyAsync(E.d_rcell, cells, sizeof(uint32_t) * nq, cudaMemcpyHostToDevice, E.stream));
+            p.qcell = E.d_rcell;
+        }
+    } else if (nq != E.total) {
+        return fail(TESS_E_INVALID, "with cells NULL, ncells must be the number of points (%u)", E.total);
+    }
+    if (mode == RQ_CLOUD) {
+        uint64_t bits;
+        memcpy(&bits, &radius, sizeof(bits));
+        if (!E.rtab_valid || bits != E.rtab_radius_bits) {
+            DiagDesc D;
+            CU(cudaMemcpyAsync(&D, E.d_desc, sizeof(D), cudaMemcpyDeviceToHost, E.stream));
+            CU(cudaStreamSynchronize(E.stream));
+            std::vector<short4> tab;
+            if (!build_radius_table(D.size, D.cpd, radius, kMaxRadiusTable, tab))
+                return fail(TESS_E_LIMIT, "radius %g reaches more than %zu bin offsets", radius, kMaxRadiusTable);
+            TRY(ensure(&E.d_rtab, E.rtab_cap, tab.size()));
+            if (!tab.empty()) {
+                CU(cudaMemcpyAsync(E.d_rtab, tab.data(), sizeof(short4) * tab.size(), cudaMemcpyHostToDevice,
+                                   E.stream));
+                CU(cudaStreamSynchronize(E.stream));
+            }
+            E.rtab_len = (uint32_t)tab.size();
+            E.rtab_radius_bits = bits;
+            E.rtab_valid = true;
+        }
+        p.rtab = E.d_rtab;
+        p.rtab_len = E.rtab_len;
+    }
+    TRY(ensure(&E.d_rcnt, E.rcnt_cap, nq + 1));
+    TRY(ensure(&E.d_roffs, E.roffs_cap, nq + 1));
+    const size_t tmp_words = csr_tmp_words((uint32_t)std::max<size_t>(nq, 1));
+    TRY(ensure(&E.d_rtmp, E.rtmp_cap, tmp_words));
+    p.count = E.d_rcnt;
+    p.offs = E.d_roffs;
+    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((nq + 7) / 8, (size_t)E.sm_count * 16));
+    CU(cudaMemsetAsync(E.d_rerr, 0, sizeof(int), E.stream));
+    uint64_t tot = 0;
+    if (nq) {
+        CU(launch_radius(p, mode, false, blocks, E.stream));
+        CU(launch_csr_offsets(E.d_rcnt, (uint32_t)nq, E.d_roffs, E.d_rtmp, E.stream));
+        CU(cudaMemcpyAsync(&tot, E.d_roffs + nq, sizeof(uint64_t), cudaMemcpyDeviceToHost, E.stream));
+        E.launches += 4;
+    }
+    int err = 0;
+    CU(cudaMemcpyAsync(&err, E.d_rerr, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
+    CU(cudaStreamSynchronize(E.stream));
+    if (err) return fail(TESS_E_INVALID, "a query cell index is out of range (n = %u)", E.total);
+    if (total) *total = (size_t)tot;
+    if (offs) {
+        if (nq) {
+            CU(cudaMemcpyAsync(offs, E.d_roffs, sizeof(uint64_t) * (nq + 1),
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, E.stream));
+        } else if (on_device) {
+            CU(cudaMemsetAsync(offs, 0, sizeof(uint64_t), E.stream));
+        } else {
+            offs[0] = 0;
+        }
+    }
+    if (!out || tot == 0) {
+        CU(cudaStreamSynchronize(E.stream));
+        return TESS_OK;
+    }
+    if (tot > cap) {
+        CU(cudaStreamSynchronize(E.stream));
+        return fail(TESS_E_CAPACITY, "%llu results, capacity %zu", (unsigned long long)tot, cap);
+    }
+    if (on_device) {
+        p.out = out;
+    } else {
+        TRY(ensure(&E.d_rout, E.rout_cap, tot));
+        p.out = E.d_rout;
+    }
+    CU(launch_radius(p, mode, true, blocks, E.stream));
+    E.launches += 1;
+    if (!on_device) CU(cudaMemcpyAsync(out, E.d_rout, sizeof(uint32_t) * tot, cudaMemcpyDeviceToHost, E.stream));
+    CU(cudaStreamSynchronize(E.stream));
+    return TESS_OK;
 }
 
 tess_status validate_box(const double* lo, const double* hi) {
@@ -937,6 +1098,36 @@ tess_status tess_results_device(tess_diagram* d, const double** volumes, const u
     if (area) *area = d->E.d_carea;
     if (total) *total = d->E.csr_total;
     return TESS_OK;
+}
+
+// ---- radius queries ----
+tess_status tess_find_cells_in_radius(tess_diagram* d, const double* xyz, size_t nq, double radius, int on_device,
+                                      uint64_t* offs, uint32_t* cells, size_t cap, size_t* total) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    return engine_radius(d->E, RQ_CELLS, false, xyz, nullptr, nq, radius, -1, on_device, offs, cells, cap, total);
+}
+
+tess_status tess_find_neighbors_in_radius(tess_diagram* d, const double* xyz, size_t nq, double radius,
+                                          int real_radius, int on_device, uint64_t* offs, uint32_t* ids,
+                                          size_t cap, size_t* total) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    return engine_radius(d->E, real_radius ? RQ_REAL_RADIUS : RQ_CELL_RADIUS, false, xyz, nullptr, nq, radius, -1,
+                         on_device, offs, ids, cap, total);
+}
+
+tess_status tess_neighbor_cloud(tess_diagram* d, const uint32_t* cells, size_t ncells, double radius,
+                                int64_t target_group, int on_device, uint64_t* offs, uint32_t* ids, size_t cap,
+                                size_t* total) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    return engine_radius(d->E, RQ_CLOUD, true, nullptr, cells, ncells, radius, target_group, on_device, offs, ids, cap,
+                         total);
+}
+
+tess_status tess_neighbor_cloud_at(tess_diagram* d, const double* xyz, size_t nq, double radius,
+                                   int64_t target_group, int on_device, uint64_t* offs, uint32_t* ids, size_t cap,
+                                   size_t* total) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    return engine_radius(d->E, RQ_CLOUD, false, xyz, nullptr, nq, radius, target_group, on_device, offs, ids, cap, total);
 }
 
 // ---- batch ----

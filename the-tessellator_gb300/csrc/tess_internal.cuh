@@ -14,6 +14,8 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 namespace tess {
@@ -141,6 +143,44 @@ constexpr int kScanThreads = 1024;
 
 cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s);
 size_t scan_tmp_words(uint64_t nitems);
+
+// ---- radius queries (tess_radius.cu) ----
+// Query kinds: find_cells_in_radius (celery.rs:753-796), the points of those
+// bins (find_neighbors_in_cell_radius, celery.rs:802-818), those within the
+// radius (find_neighbors_in_real_radius, celery.rs:825-855), and the
+// expanding-search neighbour cloud of a cell (interface.rs:348-365).
+enum RadiusMode { RQ_CELLS = 0, RQ_CELL_RADIUS = 1, RQ_REAL_RADIUS = 2, RQ_CLOUD = 3 };
+
+struct RadiusParams {
+    const DiagDesc* desc;       // the diagram (a set of one)
+    const uint32_t* delims;
+    const uint32_t* sorted;
+    const double* spx;          // FP64 positions in sorted order
+    const double* spy;
+    const double* spz;
+    const uint32_t* sgroup;     // groups in sorted order, or null (all 0)
+    const double* xyz;          // points, AoS, original order
+    const uint32_t* inv;        // point -> sorted position
+    const double* qxyz;         // query positions (AoS), or null: queries are cells
+    const uint32_t* qcell;      // cloud query cells (original index), or null: every cell
+    uint32_t nq;
+    double radius;
+    int64_t group;              // cloud only: < 0 keeps every group
+    const short4* rtab;         // cloud only: bin offsets with key <= radius, search order
+    uint32_t rtab_len;
+    uint32_t* count;            // count pass: results per query
+    const uint64_t* offs;       // fill pass: CSR offsets per query
+    uint32_t* out;              // fill pass: bin ids or original point indices
+    int* err;                   // set to 1 when a query cell is out of range
+};
+
+cudaError_t launch_radius(const RadiusParams& p, int mode, bool fill, int blocks, cudaStream_t s);
+// Bin offsets of the search order (celery.rs:418-679) whose key is at most
+// `radius`, sorted by (key, i, j, k), for a grid of cpd bins per axis with
+// the given bin sizes.  Returns false if more than max_entries would be kept
+// or enumerated.
+bool build_radius_table(const double size[3], int cpd, double radius, size_t max_entries,
+                        std::vector<short4>& out);
 
 // ---- launchers (tess_clip.cu) ----
 struct ClipParams {

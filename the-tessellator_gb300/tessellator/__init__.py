@@ -192,6 +192,66 @@ class Diagram:
         check(lib().tess_diagram_stats(self._h, C.byref(s)))
         return s.as_dict()
 
+    # ---- fixed-radius queries (celery.rs:753-855, interface.rs:348-365) ----
+    def _radius_csr(self, call, nq):
+        """Runs call(out_ptr, cap, offs_ptr, total_ref) twice: sizes, then results."""
+        offs = np.empty(nq + 1, dtype=np.uint64)
+        total = C.c_size_t(0)
+        check(call(None, 0, C.c_void_p(offs.ctypes.data), C.byref(total)))
+        out = np.empty(max(total.value, 1), dtype=np.uint32)
+        check(call(C.c_void_p(out.ctypes.data), len(out), None, C.byref(total)))
+        return offs, out[:total.value]
+
+    @staticmethod
+    def _queries(xyz):
+        q = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(-1, 3))
+        return q, C.c_void_p(q.ctypes.data if len(q) else None)
+
+    def find_cells_in_radius_batch(self, xyz, radius: float):
+        """Celery::find_cells_in_radius for each row of xyz: (offsets, bin ids)."""
+        q, qp = self._queries(xyz)
+        L = lib()
+        return self._radius_csr(lambda o, cap, offs, tot: L.tess_find_cells_in_radius(
+            self._h, qp, len(q), float(radius), 0, offs, o, cap, tot), len(q))
+
+    def find_neighbors_in_radius_batch(self, xyz, radius: float, real_radius: bool):
+        """find_neighbors_in_{cell,real}_radius for each row: (offsets, point indices)."""
+        q, qp = self._queries(xyz)
+        L = lib()
+        return self._radius_csr(lambda o, cap, offs, tot: L.tess_find_neighbors_in_radius(
+            self._h, qp, len(q), float(radius), 1 if real_radius else 0, 0, offs, o, cap, tot), len(q))
+
+    def neighbor_cloud(self, radius: float, cells=None, target_group: Optional[int] = None):
+        """Cell::compute_neighbor_cloud for the given cells (None: every cell):
+        (offsets, point indices)."""
+        L = lib()
+        if cells is None:
+            c, cp, n = None, None, self.n
+        else:
+            c = np.ascontiguousarray(np.asarray(cells, dtype=np.uint32).reshape(-1))
+            cp, n = C.c_void_p(c.ctypes.data if len(c) else None), len(c)
+        return self._radius_csr(lambda o, cap, offs, tot: L.tess_neighbor_cloud(
+            self._h, cp, n, float(radius), _group(target_group), 0, offs, o, cap, tot), n)
+
+    def neighbor_cloud_at(self, xyz, radius: float, target_group: Optional[int] = None):
+        """compute_neighbor_cloud from positions (cells made by get_cell_at_particle)."""
+        q, qp = self._queries(xyz)
+        L = lib()
+        return self._radius_csr(lambda o, cap, offs, tot: L.tess_neighbor_cloud_at(
+            self._h, qp, len(q), float(radius), _group(target_group), 0, offs, o, cap, tot), len(q))
+
+    def find_cells_in_radius(self, x: float, y: float, z: float, radius: float) -> List[int]:
+        """Celery::find_cells_in_radius (celery.rs:753-796)."""
+        return self.find_cells_in_radius_batch([[x, y, z]], radius)[1].tolist()
+
+    def find_neighbors_in_cell_radius(self, x: float, y: float, z: float, radius: float) -> List[int]:
+        """Celery::find_neighbors_in_cell_radius (celery.rs:802-818)."""
+        return self.find_neighbors_in_radius_batch([[x, y, z]], radius, False)[1].tolist()
+
+    def find_neighbors_in_real_radius(self, x: float, y: float, z: float, radius: float) -> List[int]:
+        """Celery::find_neighbors_in_real_radius (celery.rs:825-855)."""
+        return self.find_neighbors_in_radius_batch([[x, y, z]], radius, True)[1].tolist()
+
     def grid(self):
         """(cells_per_dimension, bounds {xmin, xmax, ymin, ymax, zmin, zmax})."""
         cpd = C.c_int64(0)
@@ -310,6 +370,14 @@ class Cell:
     def original_index(self) -> Optional[int]:
         """Cell::original_index (interface.rs:387-389)."""
         return self.index
+
+    def compute_neighbor_cloud(self, radius: float, target_group: Optional[int] = None) -> List[int]:
+        """Cell::compute_neighbor_cloud (interface.rs:348-365): the points of the
+        bins an expanding search from the cell's position reaches within
+        `radius` (self included), optionally only target_group's."""
+        if self.index is not None:
+            return self.diagram.neighbor_cloud(radius, [self.index], target_group)[1].tolist()
+        return self.diagram.neighbor_cloud_at([self.point], radius, target_group)[1].tolist()
 
 
 class VoronoiFace:

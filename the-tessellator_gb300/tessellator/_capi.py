@@ -29,6 +29,8 @@ EXPORTS = (
     "tess_cell_volume", "tess_cell_neighbors", "tess_cell_faces", "tess_cell_vertices",
     "tess_cell_face_vertices", "tess_cell_original_index", "tess_cell_compute",
     "tess_cell_compute_at", "tess_volumes", "tess_neighbors_csr", "tess_results_device",
+    "tess_find_cells_in_radius", "tess_find_neighbors_in_radius", "tess_neighbor_cloud",
+    "tess_neighbor_cloud_at",
     "tess_batch_create", "tess_batch_compute", "tess_batch_stats", "tess_batch_volumes",
     "tess_batch_neighbors_csr", "tess_batch_destroy", "tess_csr_offsets_noalloc",
 )
@@ -108,6 +110,13 @@ def lib():
         "tess_volumes": (st, [vp, dp]),
         "tess_neighbors_csr": (st, [vp, u64p, i32p, dp, C.c_size_t, szp]),
         "tess_results_device": (st, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), szp]),
+        "tess_find_cells_in_radius": (st, [vp, vp, C.c_size_t, C.c_double, C.c_int, vp, vp, C.c_size_t, szp]),
+        "tess_find_neighbors_in_radius": (st, [vp, vp, C.c_size_t, C.c_double, C.c_int, C.c_int, vp, vp,
+                                               C.c_size_t, szp]),
+        "tess_neighbor_cloud": (st, [vp, vp, C.c_size_t, C.c_double, C.c_int64, C.c_int, vp, vp, C.c_size_t,
+                                     szp]),
+        "tess_neighbor_cloud_at": (st, [vp, vp, C.c_size_t, C.c_double, C.c_int64, C.c_int, vp, vp,
+                                        C.c_size_t, szp]),
         "tess_batch_create": (st, [C.c_size_t, u64p, dp, dp, C.POINTER(Config), C.POINTER(vp)]),
         "tess_batch_compute": (st, [vp, C.c_int]),
         "tess_batch_stats": (st, [vp, C.POINTER(Stats)]),
