@@ -8,7 +8,10 @@ points already in HBM; `e2e` goes through the C ABI with pinned host buffers:
 upload the points, compute, read back volumes and the neighbour/area CSR.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload uniform16m|uniform1m|clustered|sc|bcc|batched] [--precision fp32|fp64]
+                    [--workload uniform16m|uniform1m|clustered|sc|bcc|batched|radius16m]
+                    [--precision fp32|fp64]
+
+`radius16m` measures the fixed-radius neighbour queries instead (queries/s).
 """
 from __future__ import annotations
 
@@ -38,15 +41,19 @@ WORKLOADS = {
     "sc": dict(n=128 ** 3, seed=5, desc="simple cubic 128^3, jitter 1e-7 spacing (seed 5)"),
     "bcc": dict(n=2 * 100 ** 3, seed=6, desc="BCC 2x100^3, jitter 1e-7 spacing (seed 6)"),
     "batched": dict(n=None, seed=4, desc="4,096 diagrams, n log-uniform in [64, 65536], boxes [0.5,2]^3 (seed 4)"),
+    "radius16m": dict(n=16_777_216, seed=2, radius=0.006,
+                      desc="find_neighbors_in_real_radius(r = 0.006) of each of 16,777,216 uniform points "
+                           "in [0,1]^3 (seed 2), queries in input order"),
 }
+RADIUS_METRIC = "radius queries/sec on 1 GB300 (find_neighbors_in_real_radius, FP64, exact)"
 
 
-def make_points(name):
+def make_points(name, points=None):
     from tessellator import workloads as W
 
     w = WORKLOADS[name]
-    if name.startswith("uniform"):
-        return W.uniform(w["n"], w["seed"]), None
+    if name.startswith("uniform") or name == "radius16m":
+        return W.uniform(points or w["n"], w["seed"]), None
     if name == "clustered":
         return W.clustered(w["n"], w["seed"]), None
     if name == "sc":
@@ -352,6 +359,141 @@ def run_ours(args, ws, rank, local):
         dist.destroy_process_group()
 
 
+def radius_cpu_baseline(pts, radius, target_seconds=10.0):
+    """The oracle's find_neighbors_in_real_radius (one thread, as the reference's
+    per-query call) on an evenly spaced sample of the queries."""
+    import oracle
+
+    n = len(pts)
+    t0 = time.perf_counter()
+    r = oracle.Diagram(pts)
+    t_build = time.perf_counter() - t0
+    m = 20000
+    t0 = time.perf_counter()
+    r.find_neighbors_in_radius(pts[np.linspace(0, n - 1, m).astype(np.int64)], radius, True)
+    rate = m / (time.perf_counter() - t0)
+    m = int(min(n, max(m, rate * target_seconds)))
+    q = pts[np.linspace(0, n - 1, m).astype(np.int64)]
+    t0 = time.perf_counter()
+    r.find_neighbors_in_radius(q, radius, True)
+    secs = time.perf_counter() - t0
+    return m / secs, (f"{m} of {n} queries (evenly spaced), 1 thread, after the grid build "
+                      f"({t_build:.2f} s, not counted)")
+
+
+def run_radius(args, ws, rank, local):
+    """Fixed-radius neighbour queries: every point asks for the points within
+    the radius (find_neighbors_in_real_radius).  A step is one batched call:
+    count pass, scan of the counts, fill pass; the grid is built once before."""
+    import torch
+
+    import tessellator as T
+
+    torch.cuda.set_device(local)
+    dist = dist_init(ws, "nccl")
+    w = WORKLOADS[args.workload]
+    pts, _ = make_points(args.workload, args.points)
+    n, radius = len(pts), w["radius"]
+    if args.points:
+        radius = w["radius"] * (w["n"] / n) ** (1.0 / 3.0)     # same mean neighbour count
+    stream = torch.cuda.Stream()
+    cfg = T.default_config(flags=T.FLAG_TIMING, stream=stream.cuda_stream, device=local)
+    host = torch.from_numpy(pts).pin_memory()
+    dev = host.to(f"cuda:{local}")
+    torch.cuda.synchronize()
+    obj = T.Diagram(device_ptr=dev.data_ptr(), n=n, config=cfg)
+    L = T.lib()
+    d_offs = torch.empty(n + 1, dtype=torch.int64, device=f"cuda:{local}")
+    cap = int(n * 20)
+    d_ids = torch.empty(cap, dtype=torch.int32, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def step_device():
+        tot = C.c_size_t(0)
+        T._capi.check(L.tess_find_neighbors_in_radius(obj._h, C.c_void_p(dev.data_ptr()), n, radius, 1, 1,
+                                                      C.c_void_p(d_offs.data_ptr()), C.c_void_p(d_ids.data_ptr()),
+                                                      cap, C.byref(tot)))
+        return tot.value
+
+    for _ in range(args.warmup):
+        total = step_device()
+    st0 = obj.stats()
+    sampler = ClockSampler(local)
+    sampler.start()
+    cnt_ms, fill_ms = [], []
+    barrier(dist)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        total = step_device()
+        s = obj.stats()
+        cnt_ms.append(s["ms_query_count"])
+        fill_ms.append(s["ms_query_fill"])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = sampler.stop()
+    ms = max_over_ranks(dist, e0.elapsed_time(e1) / args.steps, f"cuda:{local}")
+    launches = int(obj.stats()["launches"] - st0["launches"])
+
+    # e2e: host queries in, host offsets and ids out, through the C ABI
+    offs_h = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+    ids_h = torch.empty(cap, dtype=torch.int32).pin_memory()
+
+    def step_e2e():
+        tot = C.c_size_t(0)
+        T._capi.check(L.tess_find_neighbors_in_radius(obj._h, C.c_void_p(host.data_ptr()), n, radius, 1, 0,
+                                                      C.c_void_p(offs_h.data_ptr()), C.c_void_p(ids_h.data_ptr()),
+                                                      cap, C.byref(tot)))
+        return tot.value
+
+    step_e2e()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / args.steps, f"cuda:{local}")
+    e2e = {"value": n * ws / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(pts.nbytes),
+           "d2h_bytes_per_step": int(8 * (n + 1) + 4 * total), "ms_per_step": e2e_s * 1e3}
+
+    peaks, src = measured_peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    # algorithmic bytes: every query and every point position read once (24 B each),
+    # per query a count (4 B) or an offset (8 B), and 4 B per result written
+    c_ms, f_ms = float(np.mean(cnt_ms)), float(np.mean(fill_ms))
+    bytes_count = (24 + 24 + 4) * n
+    bytes_fill = (24 + 24 + 8) * n + 4 * total
+    if f_ms >= c_ms:
+        kname, kbytes, kms = "k_radius<REAL_RADIUS, fill>", bytes_fill, f_ms
+    else:
+        kname, kbytes, kms = "k_radius<REAL_RADIUS, count> + offsets scan", bytes_count, c_ms
+    ach = kbytes / (kms / 1e3) / 1e9
+    out = {
+        "metric": RADIUS_METRIC, "value": n * ws / (ms / 1e3), "unit": "queries/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w["desc"] if not args.points else f"{n} uniform points, real radius {radius:.6g}",
+                   "queries": n, "radius": radius, "results": int(total),
+                   "parallelism": "replicas",
+                   "l2": "inputs (%.0f MB of points) larger than the 129 MB L2" % (pts.nbytes / 1e6),
+                   "step": "count pass + scan + fill pass, queries and outputs resident in HBM"},
+        "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
+        "passes_ms": {"count_and_scan": c_ms, "fill": f_ms},
+        "roofline": {"kernel": kname, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                     "frac": ach / hbm, "traffic": None, "algorithmic_bytes": kbytes, "peak_source": src},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, desc = radius_cpu_baseline(pts, radius, min(args.cpu_seconds, 10.0))
+        out["cpu_baseline"] = {"value": rate, "unit": "queries/s", "cores": 1, "kind": "port", "sample": desc}
+    if rank == 0:
+        print(json.dumps(out))
+    obj.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def run_reference(args, ws, rank):
     """The reference's own CPU path is Rust (no toolchain here) and its clipper
     is unfinished, so the oracle (a C restatement of the reference algorithm)
@@ -359,6 +501,23 @@ def run_reference(args, ws, rank):
     if rank != 0:
         return
     pts, batched = make_points(args.workload)
+    if args.workload == "radius16m":
+        w = WORKLOADS[args.workload]
+        vals = []
+        for _ in range(args.warmup):
+            radius_cpu_baseline(pts, w["radius"], 2.0)
+        for _ in range(args.steps):
+            rate, desc = radius_cpu_baseline(pts, w["radius"], min(args.cpu_seconds, 10.0))
+            vals.append(rate)
+        rate = float(np.mean(vals))
+        print(json.dumps({
+            "impl": "reference", "metric": RADIUS_METRIC, "value": rate, "unit": "queries/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": len(pts) / rate * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["desc"], "queries": len(pts), "radius": w["radius"]},
+            "cpu_baseline": {"value": rate, "unit": "queries/s", "cores": 1, "kind": "port", "sample": desc},
+            "e2e": {"value": rate, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
     vals = []
     desc = ""
     for _ in range(args.warmup):
@@ -390,6 +549,8 @@ def main():
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--points", type=int, default=None,
+                    help="uniform / radius workloads only: this many points instead (profiling runs)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -398,7 +559,10 @@ def main():
     import __graft_entry__
 
     __graft_entry__.build()
-    run_ours(args, ws, rank, local)
+    if args.workload == "radius16m":
+        run_radius(args, ws, rank, local)
+    else:
+        run_ours(args, ws, rank, local)
 
 
 if __name__ == "__main__":

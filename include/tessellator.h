@@ -105,6 +105,10 @@ typedef struct {
     uint64_t new_vertices;      /* vertices created by the cuts                    */
     uint64_t windows;           /* candidate windows of up to 32 points            */
     uint64_t batches;           /* batches of up to 32 bins                        */
+    /* Last fixed-radius query (TESS_FLAG_TIMING): device times of its count
+     * pass (with the scan of the counts) and of its fill pass. */
+    double ms_query_count;
+    double ms_query_fill;
 } tess_stats;
 
 void tess_config_default(tess_config* cfg);

@@ -107,6 +107,31 @@ def test_clustered_bins(tess, oracle_mod):
             _same(d.neighbor_cloud_at(q, r), o.neighbor_cloud(q, r))
 
 
+@pytest.mark.parametrize("r", [1.0, 2.0, 2.0 ** 0.5, 3.0 ** 0.5, 0.999999999])
+def test_real_radius_ties_on_the_sphere(tess, oracle_mod, r):
+    """Integer lattice: many candidates at exactly the radius (d^2 == r^2), where
+    the FP32 pre-filter must defer to the exact FP64 test."""
+    g = np.arange(12, dtype=np.float64)
+    pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    q = np.vstack([pts[::7], pts[::11] + 0.5])
+    with tess.Diagram(pts) as d:
+        o = oracle_mod.Diagram(pts)
+        _same(d.find_neighbors_in_radius_batch(q, r, True), o.find_neighbors_in_radius(q, r, True))
+
+
+def test_real_radius_far_from_the_origin(tess, oracle_mod):
+    """Coordinates near 1e6: the FP32 filter's error band is wide and most
+    decisions fall back to FP64."""
+    rng = np.random.default_rng(75)
+    pts = 1.0e6 + rng.random((20000, 3))
+    q = 1.0e6 + rng.uniform(-0.1, 1.1, (500, 3))
+    with tess.Diagram(pts) as d:
+        o = oracle_mod.Diagram(pts)
+        for r in (0.03, 0.1):
+            _same(d.find_neighbors_in_radius_batch(q, r, True), o.find_neighbors_in_radius(q, r, True))
+            _same(d.find_cells_in_radius_batch(q, r), o.find_cells_in_radius(q, r))
+
+
 def test_real_radius_million_points(tess, oracle_mod):
     """1,000,000 points, 100,000 queries, radius 0.012 (about 9 neighbours each)."""
     rng = np.random.default_rng(73)
@@ -116,6 +141,21 @@ def test_real_radius_million_points(tess, oracle_mod):
         got = d.find_neighbors_in_radius_batch(q, 0.012, True)
     _same(got, oracle_mod.Diagram(pts).find_neighbors_in_radius(q, 0.012, True))
     assert 5 < len(got[1]) / len(q) < 12
+
+
+def test_large_batches_in_spatial_order(tess, oracle_mod):
+    """Batches of 65,536 queries or more are processed in coarse-bin order;
+    results stay in query order."""
+    rng = np.random.default_rng(74)
+    pts = rng.random((300_000, 3))
+    cells = rng.permutation(len(pts)).astype(np.uint32)[:150_000]
+    q = rng.uniform(-0.05, 1.05, (120_000, 3))
+    with tess.Diagram(pts) as d:
+        o = oracle_mod.Diagram(pts)
+        _same(d.neighbor_cloud(0.0002, cells), o.neighbor_cloud(pts[cells], 0.0002))
+        _same(d.neighbor_cloud_at(q, 0.0002), o.neighbor_cloud(q, 0.0002))
+        _same(d.find_neighbors_in_radius_batch(q, 0.02, True), o.find_neighbors_in_radius(q, 0.02, True))
+        _same(d.find_cells_in_radius_batch(q, 0.01), o.find_cells_in_radius(q, 0.01))
 
 
 # ---- the C ABI's contract ---------------------------------------------------------

@@ -143,6 +143,27 @@ struct Engine {
     uint64_t rtab_radius_bits = 0;
     int* d_rerr = nullptr;
     int sm_count = 0;
+    unsigned long long* d_bnd = nullptr;   // bin boundaries per axis (3 x cpd order codes)
+    size_t bnd_cap = 0;
+    bool bnd_valid = false;
+    DiagDesc hgrid{};             // host copy of the device-written grid fields
+    bool hgrid_valid = false;
+    int16_t* d_gtab = nullptr;    // gap table of the last box-query radius
+    size_t gtab_cap = 0;
+    bool gtab_valid = false, gtab_present = false;
+    uint64_t gtab_radius_bits = 0;
+    int gtab_dim[3] = {};
+    // spatial order of large query batches
+    uint32_t* d_qbin = nullptr;
+    uint32_t* d_qrank = nullptr;
+    uint32_t* d_qorder = nullptr;
+    size_t qord_cap = 0, qrank_cap = 0, qorder_cap = 0;
+    uint32_t* d_qcnt = nullptr;
+    size_t qcnt_cap = 0;
+    uint64_t* d_qcoff = nullptr;
+    size_t qcoff_cap = 0;
+    uint64_t* d_qtmp = nullptr;
+    size_t qtmp_cap = 0;
     // state
     bool built = false;
     bool computed = false;
@@ -171,7 +192,7 @@ struct Engine {
         dfree(d_counters); dfree(d_work); dfree(d_offs); dfree(d_cnbr); dfree(d_carea); dfree(d_csr_tmp);
         dfree(d_geo); dfree(d_one);
         dfree(d_rq); dfree(d_rcell); dfree(d_rcnt); dfree(d_roffs); dfree(d_rtmp); dfree(d_rout); dfree(d_rtab);
-        dfree(d_rerr);
+        dfree(d_rerr); dfree(d_gtab); dfree(d_bnd); dfree(d_qbin); dfree(d_qrank); dfree(d_qorder); dfree(d_qcnt); dfree(d_qcoff); dfree(d_qtmp);
         if (own_stream && stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -376,6 +397,9 @@ tess_status engine_build(Engine& E, bool check) {
     E.computed = false;
     E.csr_valid = false;
     E.rtab_valid = false;
+    E.gtab_valid = false;
+    E.hgrid_valid = false;
+    E.bnd_valid = false;
     return TESS_OK;
 }
 
@@ -478,6 +502,13 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
     CU(cudaSetDevice(E.device));
     const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
     cudaEvent_t ev[3] = {};
+    struct EventGuard {
+        cudaEvent_t* e;
+        ~EventGuard() {
+            for (int i = 0; i < 3; ++i)
+                if (e[i]) cudaEventDestroy(e[i]);
+        }
+    } guard{ev};
     if (timing)
         for (auto& e : ev) CU(cudaEventCreate(&e));
     for (int attempt = 0; attempt < 4; ++attempt) {
@@ -634,6 +665,11 @@ tess_status ensure(T** p, size_t& cap, size_t need) {
 
 // Largest search-order prefix a neighbour-cloud call may enumerate.
 constexpr size_t kMaxRadiusTable = (size_t)1 << 26;
+// Query batches at least this large are processed in spatial order.
+constexpr size_t kOrderMin = 65536;
+// Largest gap table (entries of int16) for box queries; beyond it the
+// kernel evaluates the gap distance per bin in FP64.
+constexpr size_t kMaxGapTable = 65536;
 
 // Fixed-radius queries (tess_radius.cu) over nq queries: positions qxyz, or
 // cells (cloud only; null = every cell).  Count pass, scan, then the fill
@@ -684,13 +720,47 @@ tess_status engine_radius(Engine& E, int mode, bool by_cell, const double* qxyz,
     } else if (nq != E.total) {
         return fail(TESS_E_INVALID, "with cells NULL, ncells must be the number of points (%u)", E.total);
     }
-    if (mode == RQ_CLOUD) {
-        uint64_t bits;
-        memcpy(&bits, &radius, sizeof(bits));
-        if (!E.rtab_valid || bits != E.rtab_radius_bits) {
-            DiagDesc D;
-            CU(cudaMemcpyAsync(&D, E.d_desc, sizeof(D), cudaMemcpyDeviceToHost, E.stream));
+    uint64_t bits;
+    memcpy(&bits, &radius, sizeof(bits));
+    const bool need_cloud_tab = mode == RQ_CLOUD && (!E.rtab_valid || bits != E.rtab_radius_bits);
+    const bool need_gap_tab = mode != RQ_CLOUD && (!E.gtab_valid || bits != E.gtab_radius_bits);
+    if ((need_cloud_tab || need_gap_tab) && !E.hgrid_valid) {
+        CU(cudaMemcpyAsync(&E.hgrid, E.d_desc, sizeof(DiagDesc), cudaMemcpyDeviceToHost, E.stream));
+        CU(cudaStreamSynchronize(E.stream));
+        E.hgrid_valid = true;
+    }
+    const DiagDesc& D = E.hgrid;
+    if (need_gap_tab) {
+        std::vector<int16_t> gt;
+        E.gtab_present = build_gap_table(D.size, D.inv, D.cpd, radius, kMaxGapTable, gt, &E.gtab_dim[0],
+                                         &E.gtab_dim[1], &E.gtab_dim[2]);
+        if (E.gtab_present) {
+            TRY(ensure(&E.d_gtab, E.gtab_cap, gt.size()));
+            CU(cudaMemcpyAsync(E.d_gtab, gt.data(), sizeof(int16_t) * gt.size(), cudaMemcpyHostToDevice, E.stream));
             CU(cudaStreamSynchronize(E.stream));
+        }
+        E.gtab_radius_bits = bits;
+        E.gtab_valid = true;
+    }
+    if (mode != RQ_CLOUD && E.gtab_present) {
+        p.gtab = E.d_gtab;
+        p.gtab_x = E.gtab_dim[0];
+        p.gtab_y = E.gtab_dim[1];
+        p.gtab_z = E.gtab_dim[2];
+    }
+    if (!E.bnd_valid) {
+        const int cpd = E.hdesc[0].cpd;
+        TRY(ensure(&E.d_bnd, E.bnd_cap, 3 * (size_t)cpd));
+        CU(launch_axis_bounds(E.d_desc, cpd, E.d_bnd, E.stream));
+        E.launches += 1;
+        E.bnd_valid = true;
+    }
+    p.bnd = E.d_bnd;
+    p.shi = E.d_shi;
+    const double r2 = radius * radius;
+    p.f32_filter = mode == RQ_REAL_RADIUS && std::isfinite(radius) && r2 >= 1e-30 && r2 <= 1e36;
+    if (mode == RQ_CLOUD) {
+        if (need_cloud_tab) {
             std::vector<short4> tab;
             if (!build_radius_table(D.size, D.cpd, radius, kMaxRadiusTable, tab))
                 return fail(TESS_E_LIMIT, "radius %g reaches more than %zu bin offsets", radius, kMaxRadiusTable);
@@ -715,16 +785,51 @@ tess_status engine_radius(Engine& E, int mode, bool by_cell, const double* qxyz,
     p.offs = E.d_roffs;
     const int blocks = (int)std::max<size_t>(1, std::min<size_t>((nq + 7) / 8, (size_t)E.sm_count * 16));
     CU(cudaMemsetAsync(E.d_rerr, 0, sizeof(int), E.stream));
+    const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
+    cudaEvent_t ev[3] = {};
+    if (timing)
+        for (auto& e : ev) CU(cudaEventCreate(&e));
+    E.stats.ms_query_count = E.stats.ms_query_fill = 0.0;
     uint64_t tot = 0;
     if (nq) {
+        if (timing) CU(cudaEventRecord(ev[0], E.stream));
+        if (nq >= kOrderMin && (p.qxyz || p.qcell)) {
+            // process large batches in coarse-bin order: neighbouring warps then
+            // read the same candidate bins
+            QueryOrder o{};
+            o.cpdc = (E.hdesc[0].cpd + 1) / 2;
+            o.ncoarse = (uint32_t)o.cpdc * (uint32_t)o.cpdc * (uint32_t)o.cpdc;
+            TRY(ensure(&E.d_qbin, E.qord_cap, nq));
+            TRY(ensure(&E.d_qrank, E.qrank_cap, nq));
+            TRY(ensure(&E.d_qorder, E.qorder_cap, nq));
+            TRY(ensure(&E.d_qcnt, E.qcnt_cap, o.ncoarse));
+            TRY(ensure(&E.d_qcoff, E.qcoff_cap, (size_t)o.ncoarse + 1));
+            TRY(ensure(&E.d_qtmp, E.qtmp_cap, csr_tmp_words(o.ncoarse)));
+            o.qbin = E.d_qbin;
+            o.qrank = E.d_qrank;
+            o.order = E.d_qorder;
+            o.cnt = E.d_qcnt;
+            o.coff = E.d_qcoff;
+            o.scan_tmp = E.d_qtmp;
+            const int eblocks = (int)std::min<size_t>((nq + 255) / 256, (size_t)E.sm_count * 8);
+            CU(launch_query_order(p, o, eblocks, E.stream));
+            E.launches += 5;
+            p.qorder = E.d_qorder;
+        }
         CU(launch_radius(p, mode, false, blocks, E.stream));
         CU(launch_csr_offsets(E.d_rcnt, (uint32_t)nq, E.d_roffs, E.d_rtmp, E.stream));
+        if (timing) CU(cudaEventRecord(ev[1], E.stream));
         CU(cudaMemcpyAsync(&tot, E.d_roffs + nq, sizeof(uint64_t), cudaMemcpyDeviceToHost, E.stream));
         E.launches += 4;
     }
     int err = 0;
     CU(cudaMemcpyAsync(&err, E.d_rerr, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
     CU(cudaStreamSynchronize(E.stream));
+    if (timing && nq) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        E.stats.ms_query_count = ms;
+    }
     if (err) return fail(TESS_E_INVALID, "a query cell index is out of range (n = %u)", E.total);
     if (total) *total = (size_t)tot;
     if (offs) {
@@ -751,10 +856,17 @@ tess_status engine_radius(Engine& E, int mode, bool by_cell, const double* qxyz,
         TRY(ensure(&E.d_rout, E.rout_cap, tot));
         p.out = E.d_rout;
     }
+    if (timing) CU(cudaEventRecord(ev[1], E.stream));
     CU(launch_radius(p, mode, true, blocks, E.stream));
+    if (timing) CU(cudaEventRecord(ev[2], E.stream));
     E.launches += 1;
     if (!on_device) CU(cudaMemcpyAsync(out, E.d_rout, sizeof(uint32_t) * tot, cudaMemcpyDeviceToHost, E.stream));
     CU(cudaStreamSynchronize(E.stream));
+    if (timing) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[1], ev[2]);
+        E.stats.ms_query_fill = ms;
+    }
     return TESS_OK;
 }
 

@@ -172,7 +172,35 @@ struct RadiusParams {
     const uint64_t* offs;       // fill pass: CSR offsets per query
     uint32_t* out;              // fill pass: bin ids or original point indices
     int* err;                   // set to 1 when a query cell is out of range
+    const uint32_t* qorder;     // processing order of the queries (spatially sorted), or null
+    const float* shi;           // FP32 high parts of the sorted positions (AoS), for the FP32 filter
+    int f32_filter;             // real radius: pre-filter candidates in FP32 (radius in range)
+    // check_cell_in_range as a table: for gaps gx <= gtab_x, gy <= gtab_y, the
+    // largest gz <= gtab_z whose squared gap distance is within radius^2
+    // (-1: none); null: the FP64 formula per bin
+    const int16_t* gtab;
+    int gtab_x, gtab_y, gtab_z;
+    // bin boundaries per axis: bnd[a * cpd + i] (1 <= i < cpd) is the order
+    // code (ord_enc) of the smallest double whose axis_index is >= i
+    const unsigned long long* bnd;
 };
+
+// Fills RadiusParams::bnd for diagram 0 (3 * cpd entries).
+cudaError_t launch_axis_bounds(const DiagDesc* desc, int cpd, unsigned long long* bnd, cudaStream_t s);
+
+// Spatial processing order for large query batches: a counting sort of the
+// queries by the coarse bin (2 x 2 x 2 grid bins) holding their position.
+struct QueryOrder {
+    uint32_t* qbin;             // [nq] coarse bin of each query
+    uint32_t* qrank;            // [nq] arrival rank within its coarse bin
+    uint32_t* cnt;              // [ncoarse] queries per coarse bin
+    uint64_t* coff;             // [ncoarse + 1] offsets
+    uint64_t* scan_tmp;         // csr_tmp_words(ncoarse)
+    uint32_t* order;            // [nq] the result
+    uint32_t ncoarse;
+    int cpdc;                   // coarse bins per dimension
+};
+cudaError_t launch_query_order(const RadiusParams& p, const QueryOrder& o, int blocks, cudaStream_t s);
 
 cudaError_t launch_radius(const RadiusParams& p, int mode, bool fill, int blocks, cudaStream_t s);
 // Bin offsets of the search order (celery.rs:418-679) whose key is at most
@@ -181,6 +209,10 @@ cudaError_t launch_radius(const RadiusParams& p, int mode, bool fill, int blocks
 // or enumerated.
 bool build_radius_table(const double size[3], int cpd, double radius, size_t max_entries,
                         std::vector<short4>& out);
+// The gap table of RadiusParams::gtab for this radius; false if the radius is
+// not finite and non-negative or the table would exceed max_entries.
+bool build_gap_table(const double size[3], const double inv[3], int cpd, double radius, size_t max_entries,
+                     std::vector<int16_t>& out, int* gx, int* gy, int* gz);
 
 // ---- launchers (tess_clip.cu) ----
 struct ClipParams {
