@@ -148,3 +148,26 @@ def test_batch_matches_single_diagrams(tess, oracle_mod):
         b.compute(prec)
         assert np.array_equal(b.volumes(), vol)
         b.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_timing_flag(tess, oracle_mod, prec):
+    """With TESS_FLAG_TIMING the per-pass times are recorded and every later
+    call still succeeds (twice in a row, CSR and a radius query included)."""
+    rng = np.random.default_rng(33)
+    pts = rng.random((30000, 3))
+    cfg = tess.default_config(flags=tess.FLAG_TIMING)
+    with tess.Diagram(pts, container=tess.Polyhedron(0, 0, 0, 1, 1, 1), config=cfg) as d:
+        for _ in range(2):
+            d.rebuild()
+            d.compute_all(prec)
+            offs, nbr, area = d.neighbors_csr()
+            st = d.stats()
+            assert st["ms_grid"] > 0 and st["ms_clip"] > 0 and st["ms_csr"] > 0
+            d.find_neighbors_in_radius_batch(pts[:100], 0.03, True)
+            assert d.stats()["ms_query_count"] > 0 and d.stats()["ms_query_fill"] > 0
+        vol = d.volumes()
+    rvol, roffs, rids, _, _, _ = oracle_mod.Diagram(pts, lo=[0, 0, 0], hi=[1, 1, 1]).compute_all()
+    assert offs.astype(np.int64).tolist() == roffs.tolist()
+    assert nbr.astype(np.int64).tolist() == rids.tolist()
+    np.testing.assert_allclose(vol, rvol, rtol=1e-6 if prec == "fp32" else 1e-12)

@@ -389,6 +389,7 @@ tess_status engine_build(Engine& E, bool check) {
         CU(cudaEventSynchronize(e1));
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
+        (void)cudaGetLastError();   // best-effort timing leaves no error behind
         E.stats.ms_grid = ms;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -545,9 +546,10 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
             float a = 0, b = 0;
             cudaEventElapsedTime(&a, ev[0], ev[1]);
             cudaEventElapsedTime(&b, ev[1], ev[2]);
+            (void)cudaGetLastError();   // timing is best effort; leave no error behind
             E.stats.ms_clip = a;
             E.stats.ms_rerun = b;
-            for (auto& e : ev) cudaEventDestroy(e);
+            // the events are destroyed by the guard at scope exit
         }
         E.computed = true;
         E.csr_valid = false;
@@ -605,6 +607,7 @@ tess_status engine_csr(Engine& E) {
         CU(cudaEventSynchronize(e1));
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
+        (void)cudaGetLastError();   // best-effort timing leaves no error behind
         E.stats.ms_csr = ms;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -828,6 +831,7 @@ tess_status engine_radius(Engine& E, int mode, bool by_cell, const double* qxyz,
     if (timing && nq) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        (void)cudaGetLastError();   // best-effort timing leaves no error behind
         E.stats.ms_query_count = ms;
     }
     if (err) return fail(TESS_E_INVALID, "a query cell index is out of range (n = %u)", E.total);
@@ -865,6 +869,7 @@ tess_status engine_radius(Engine& E, int mode, bool by_cell, const double* qxyz,
     if (timing) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ev[1], ev[2]);
+        (void)cudaGetLastError();   // best-effort timing leaves no error behind
         E.stats.ms_query_fill = ms;
     }
     return TESS_OK;
@@ -1323,6 +1328,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
     if (timing) {
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
+        (void)cudaGetLastError();   // best-effort timing leaves no error behind
         E.stats.ms_clip = ms;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);

@@ -503,8 +503,15 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
     if (!anyo) return 0;
     int f = C.np;
     if (f >= S_t::P) {
-        f = recycle_plane<T, K>(S, C, lane);
-        if (f < 0) return -ST_PCAP;
+        // Only the largest capacity recycles plane ids: a call here costs the
+        // smaller instantiations' hot path registers even when never taken,
+        // and their cells re-run at the next capacity instead.
+        if constexpr (K == 8) {
+            f = recycle_plane<T, K>(S, C, lane);
+            if (f < 0) return -ST_PCAP;
+        } else {
+            return -ST_PCAP;
+        }
     }
     int R = 0;
 #pragma unroll
@@ -1191,7 +1198,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         }
         // volume: sum of pyramids from the site, area * height / 3
         // (compute_volume, polyhedron.rs:838-855)
-        vol = warp_sum_d(vpart) / 3.0;
+        vol = GUARD ? warp_sum_d(vpart) * (1.0 / 3.0) : warp_sum_d(vpart) / 3.0;
 #pragma unroll
         for (int r = 0; r < R; ++r) F += __popc(__ballot_sync(FULL, fdegr[r] > 0));
         // Every vertex has three faces: V - E + F = 2 with E = 3V/2.
