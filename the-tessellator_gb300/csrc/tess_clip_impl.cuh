@@ -164,6 +164,20 @@ __device__ __forceinline__ double sdist(double nx, double ny, double nz, double 
     return fma(nx, x, fma(ny, y, fma(nz, z, -off)));
 }
 
+// Upper bound of sqrt(x) for the FP32 form's bounds (cell radius, plane
+// norms): rsqrt is within 2 ulp and the product adds half an ulp, so the
+// 2^-20 inflation keeps it above the exact root.  0 and NaN give 0, +inf
+// stays +inf.  Double inputs keep the IEEE square root.
+__device__ __forceinline__ float sqrt_up(float x) {
+    const float r = x * rsqrtf(x) * 1.00000095367431640625f;
+    return x > 0.f ? (x < INFINITY ? r : x) : 0.f;
+}
+__device__ __forceinline__ double sqrt_up(double x) { return sqrt(x); }
+// Reciprocal for the FP32 Cramer solves: the hardware approximation (about
+// 1 ulp); its error sits well inside the vertex error bound kVertexErr.
+__device__ __forceinline__ float recip(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double recip(double x) { return 1.0 / x; }
+
 // Bisector of the site (origin) and r (halfway_from_origin_to, vector3.rs:223-239).
 // FP32 form: the same plane unnormalised, n = r, off = r.r / 2; rn = |r|.
 __device__ __forceinline__ void bisector(float rx, float ry, float rz, float r2, float& nx, float& ny,
@@ -172,7 +186,7 @@ __device__ __forceinline__ void bisector(float rx, float ry, float rz, float r2,
     ny = ry;
     nz = rz;
     off = 0.5f * r2;
-    rn = sqrtf(r2);
+    rn = sqrt_up(r2);     // an upper bound: it only widens the guard band
 }
 __device__ __forceinline__ void bisector(double rx, double ry, double rz, double r2, double& nx,
                                          double& ny, double& nz, double& off, double& rn) {
@@ -360,12 +374,12 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
                 const T fax = ny * az - nz * ay, fay = nz * ax - nx * az, faz = nx * ay - ny * ax;
                 const T abx = ay * bz - az * by, aby = az * bx - ax * bz, abz = ax * by - ay * bx;
                 const T det = ax * bfx + ay * bfy + az * bfz;
-                const T inv = (T)1 / det;
+                const T inv = recip(det);
                 px = (ah * bfx + bh * fax + off * abx) * inv;
                 py = (ah * bfy + bh * fay + off * aby) * inv;
                 pz = (ah * bfz + bh * faz + off * abz) * inv;
-                const T dhat = fabs(det) / (S.pn[a] * S.pn[b] * rn);
-                pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) / max(dhat, (T)1e-30);
+                // e = kVertexErr |x|_1 / dhat, dhat = |det| / (|n_a| |n_b| |n_f|)
+                pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) * (S.pn[a] * S.pn[b] * rn) * fabs(inv);
                 if (!(pe < (T)1e30)) pe = (T)1e30;
             } else {
                 const T den = xsd - ysd;
@@ -562,12 +576,12 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
                 const T fax = ny * az - nz * ay, fay = nz * ax - nx * az, faz = nx * ay - ny * ax;
                 const T abx = ay * bz - az * by, aby = az * bx - ax * bz, abz = ax * by - ay * bx;
                 const T det = ax * bfx + ay * bfy + az * bfz;
-                const T inv = (T)1 / det;
+                const T inv = recip(det);
                 px = (ah * bfx + bh * fax + off * abx) * inv;
                 py = (ah * bfy + bh * fay + off * aby) * inv;
                 pz = (ah * bfz + bh * faz + off * abz) * inv;
-                const T dhat = fabs(det) / (S.pn[a] * S.pn[b] * rn);
-                pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) / max(dhat, (T)1e-30);
+                // e = kVertexErr |x|_1 / dhat, dhat = |det| / (|n_a| |n_b| |n_f|)
+                pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) * (S.pn[a] * S.pn[b] * rn) * fabs(inv);
                 if (!(pe < (T)1e30)) pe = (T)1e30;
             } else {
                 const T xx = S.vx[x], xy = S.vy[x], xz = S.vz[x], xsd = S.vsd[x];
@@ -657,7 +671,7 @@ __device__ __forceinline__ T live_r2(const CellRegs<T, K>& C, int lane) {
         if ((C.lm[k] >> lane) & 1u) {
             T q = C.vx[k] * C.vx[k] + C.vy[k] * C.vy[k] + C.vz[k] * C.vz[k];
             if (sizeof(T) == 4) {
-                const T r = sqrt(q) + C.ve[k];
+                const T r = sqrt_up(q) + C.ve[k];
                 q = r * r;
             }
             r2 = max(r2, q);
@@ -791,7 +805,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     __syncwarp();
     T R2 = live_r2(C, lane);
     // cR: bound on the FP32 rounding of one plane test, relative to the cell radius
-    T cR = (T)P.guard_rel * sqrt(R2);
+    T cR = (T)P.guard_rel * sqrt_up(R2);
     int status = ST_OK;
 
     // ---- the walk over bins in shell order (celery.rs:1023-1075) ----
@@ -882,7 +896,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     ++W.cuts;
                     W.newv += (unsigned)(r - 1);
                     R2 = live_r2(C, lane);
-                    cR = (T)P.guard_rel * sqrt(R2);
+                    cR = (T)P.guard_rel * sqrt_up(R2);
                 }
             }
         }
@@ -1115,7 +1129,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     const float cax = cy_ * az_ - cz_ * ay_, cay = cz_ * ax_ - cx_ * az_, caz = cx_ * ay_ - cy_ * ax_;
                     const float abx = ay_ * bz_ - az_ * by_, aby = az_ * bx_ - ax_ * bz_, abz = ax_ * by_ - ay_ * bx_;
                     const float det = ax_ * bcx + ay_ * bcy + az_ * bcz;
-                    const float inv = 1.0f / det;
+                    const float inv = recip(det);
                     const float ddx = (ra * bcx + rb * cax + rc * abx) * inv;
                     const float ddy = (ra * bcy + rb * cay + rc * aby) * inv;
                     const float ddz = (ra * bcz + rb * caz + rc * abz) * inv;
