@@ -63,31 +63,45 @@ struct Smem {
     static constexpr int V = 32 * K;                                 // vertex slots
     static constexpr int P = (32 * K + 32) < 254 ? (32 * K + 32) : 254;  // planes (< 0xFF)
     static constexpr int VUSE = V < 255 ? V : 255;                    // slot 255 is the map sentinel
-    T px[P], py[P], pz[P], pd[P];     // plane: normal, offset (n.x = offset)
-    T pn[P];                          // |normal| (1 for the FP64 form and the walls)
-    T vx[V], vy[V], vz[V], vsd[V];    // vertex mirror, signed distances
+    static constexpr int PF = sizeof(T) == 4 ? P : 1;
+    static constexpr int VF = sizeof(T) == 4 ? V : 1;
+    // live through the whole cell
+    T vx[V], vy[V], vz[V];            // vertex mirror
     int32_t pid[P];                   // neighbour id (local original index) or wall code
     uint32_t psrc[P];                 // sorted index of the point that made the plane
     uint32_t tri[V];                  // planes a | b << 8 | c << 16
     uint32_t adj[V];                  // neighbours n0 | n1 << 8 | n2 << 16
-    uint32_t fdeg[P];                 // finalize: live vertices per face
-    uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
-    uint32_t cbeg2[32], ccnt[32];     // second-half bins: starts and prefix counts
-    uint16_t items[V + 32];           // boundary edges of a cut: slot | edge << 8
-    uint8_t fl[V + 32];               // free-slot stack (top = lowest free slot)
-    uint32_t pused[(P + 31) / 32];    // plane recycling: planes referenced by live vertices
-    int32_t flist[P];                 // finalize: compacted face ids
-    uint8_t fsta[P];                  // finalize: one vertex of each face
-    uint8_t mapf[P], maps[P];         // new-vertex ring maps
-    uint8_t rank2p[P];                // geometry output: rank -> plane
-    // FP32 form only: FP64 face planes {n, h} (n.x = h) and their distance
-    // from the site, and per-vertex FP32 corrections to the FP64 position.
-    static constexpr int PF = sizeof(T) == 4 ? P : 1;
-    static constexpr int VF = sizeof(T) == 4 ? V : 1;
-    double qx[PF], qy[PF], qz[PF], qh[PF];
-    float fqx[PF], fqy[PF], fqz[PF], qdist[PF];
-    float dx[VF], dy[VF], dz[VF];
-    float ve[VF];                     // vertex error bounds (mirror of CellRegs::ve)
+    // The walk's working arrays and the finalize's share storage: no array
+    // of one phase is read in the other, and every walk array is set up
+    // again at the start of each cell.
+    union {
+        struct {                      // walk
+            T px[P], py[P], pz[P], pd[P];     // plane: normal, offset (n.x = offset)
+            T pn[P];                          // |normal| (1 for the FP64 form and the walls)
+            T vsd[V];                         // signed distances of the current cut
+            uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
+            uint32_t cbeg2[32], ccnt[32];     // second-half bins: starts and prefix counts
+            uint32_t pused[(P + 31) / 32];    // plane recycling: planes referenced by live vertices
+            float ve[VF];                     // vertex error bounds (mirror of CellRegs::ve)
+            uint16_t items[V + 32];           // boundary edges of a cut: slot | edge << 8
+            uint8_t fl[V + 32];               // free-slot stack (top = lowest free slot)
+            // new-vertex ring maps: gen << 8 | slot; entries with another
+            // cut's tag are stale
+            uint16_t mapf[P], maps[P];
+        };
+        struct {                      // finalize
+            // FP32 form only: FP64 face planes {n, h} (n.x = h) and their
+            // distance from the site, and per-vertex FP32 corrections to the
+            // FP64 position
+            double qx[PF], qy[PF], qz[PF], qh[PF];
+            float fqx[PF], fqy[PF], fqz[PF], qdist[PF];
+            float dx[VF], dy[VF], dz[VF];
+            uint32_t fdeg[P];                 // live vertices per face
+            int32_t flist[P];                 // compacted face ids
+            uint8_t fsta[P];                  // one vertex of each face
+            uint8_t rank2p[P];                // geometry output: rank -> plane
+        };
+    };
 };
 
 __device__ __forceinline__ unsigned warp_incl_scan_u(unsigned v, int lane) {
@@ -213,6 +227,7 @@ struct CellRegs {
     uint32_t lm[K];   // live masks (warp-uniform)
     int np;           // planes used (warp-uniform)
     int nfree;        // entries on the free-slot stack (warp-uniform)
+    uint32_t gen;     // tag of the current cut in the ring maps, 0..255 (warp-uniform)
 };
 
 // The general form of a cut (more than 32 edges leave the Outside
@@ -269,7 +284,7 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const int s = k * 32 + lane;
-        if ((C.lm[k] >> lane) & 1u) S.vsd[s] = sd[k];
+        if (!GUARD && ((C.lm[k] >> lane) & 1u)) S.vsd[s] = sd[k];   // read by the FP64 interpolation
         xt[k] = 0;
         xa[k] = 0;
         if ((om[k] >> lane) & 1u) {
@@ -402,8 +417,8 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
                            : (plane_of(ty, 1) == b && plane_of(ty, 2) == a) ? 1
                                                                             : 2;
             reinterpret_cast<uint8_t*>(S.adj)[4 * y + yi] = (uint8_t)slot;
-            S.mapf[a] = (uint8_t)slot;
-            S.maps[b] = (uint8_t)slot;
+            S.mapf[a] = (uint16_t)((C.gen << 8) | (uint32_t)slot);
+            S.maps[b] = (uint16_t)((C.gen << 8) | (uint32_t)slot);
             S.adj[slot] = (uint32_t)y;
 #pragma unroll
             for (int k = 0; k < K; ++k)
@@ -422,18 +437,12 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
             const int s = k * 32 + lane;
             const uint32_t tt = S.tri[s];
             const int a = plane_of(tt, 0), b = plane_of(tt, 1);
-            const int n1 = S.mapf[b], n2 = S.maps[a];
-            bad |= (S.mapf[a] != s) || (S.maps[b] != s) || n1 == 0xFF || n2 == 0xFF;
+            const uint32_t tag = C.gen << 8;
+            const uint32_t mb = S.mapf[b], ma = S.maps[a];
+            const int n1 = (mb & 0xFF00u) == tag ? (int)(mb & 0xFFu) : 0xFF;
+            const int n2 = (ma & 0xFF00u) == tag ? (int)(ma & 0xFFu) : 0xFF;
+            bad |= (S.mapf[a] != (tag | (uint32_t)s)) || (S.maps[b] != (tag | (uint32_t)s)) || n1 == 0xFF || n2 == 0xFF;
             S.adj[s] = (S.adj[s] & 0xFFu) | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
-        }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        if ((newm[k] >> lane) & 1u) {
-            const uint32_t tt = S.tri[k * 32 + lane];
-            S.mapf[plane_of(tt, 0)] = 0xFF;
-            S.maps[plane_of(tt, 1)] = 0xFF;
         }
     }
     if (__any_sync(FULL, bad)) return -ST_DEGEN;
@@ -527,6 +536,16 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             return -ST_PCAP;
         }
     }
+    // a new tag for this cut's ring-map entries; every 256 cuts the maps are
+    // cleared, so a stale entry never carries the current tag
+    C.gen = (C.gen + 1) & 0xFFu;
+    if (C.gen == 0) {
+        for (int i = lane; i < S_t::P; i += 32) {
+            S.mapf[i] = 0xFFFF;
+            S.maps[i] = 0xFFFF;
+        }
+        __syncwarp();
+    }
     int R = 0;
 #pragma unroll
     for (int k = 0; k < K; ++k) R += __popc(om[k]);
@@ -539,7 +558,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             const int s = k * 32 + lane;
-            if ((C.lm[k] >> lane) & 1u) S.vsd[s] = sd[k];
+            if (!GUARD && ((C.lm[k] >> lane) & 1u)) S.vsd[s] = sd[k];   // read by the FP64 interpolation
             if ((om[k] >> lane) & 1u) S.fl[base + before + __popc(om[k] & ((1u << lane) - 1u))] = (uint8_t)s;
             before += __popc(om[k]);
         }
@@ -606,21 +625,20 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
                            : (plane_of(ty, 1) == b && plane_of(ty, 2) == a) ? 1
                                                                             : 2;
             reinterpret_cast<uint8_t*>(S.adj)[4 * y + yi] = (uint8_t)slot;
-            S.mapf[a] = (uint8_t)slot;
-            S.maps[b] = (uint8_t)slot;
+            S.mapf[a] = (uint16_t)((C.gen << 8) | (uint32_t)slot);
+            S.maps[b] = (uint16_t)((C.gen << 8) | (uint32_t)slot);
         }
         __syncwarp();
         if (bnd) {
             // across (b, f): the new vertex whose first plane is b; across
-            // (f, a): the one whose second plane is a
-            const int n1 = S.mapf[b], n2 = S.maps[a];
-            bad = (S.mapf[a] != slot) || (S.maps[b] != slot) || n1 == 0xFF || n2 == 0xFF;
+            // (f, a): the one whose second plane is a (entries of this cut only)
+            const uint32_t tag = C.gen << 8;
+            const uint32_t mb = S.mapf[b], ma = S.maps[a];
+            const int n1 = (mb & 0xFF00u) == tag ? (int)(mb & 0xFFu) : 0xFF;
+            const int n2 = (ma & 0xFF00u) == tag ? (int)(ma & 0xFFu) : 0xFF;
+            bad = (S.mapf[a] != (tag | (uint32_t)slot)) || (S.maps[b] != (tag | (uint32_t)slot)) || n1 == 0xFF ||
+                  n2 == 0xFF;
             S.adj[slot] = (uint32_t)y | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
-        }
-        __syncwarp();
-        if (bnd) {
-            S.mapf[a] = 0xFF;
-            S.maps[b] = 0xFF;
         }
         if (__any_sync(FULL, bad)) return -ST_DEGEN;
         C.nfree = base + R - B;
@@ -636,15 +654,15 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
                 if constexpr (GUARD) C.ve[k] = S.ve[s];
             }
         }
-        // the plane, one field per lane
-        if (lane < 7) {
-            if (lane == 0) S.px[f] = nx;
-            else if (lane == 1) S.py[f] = ny;
-            else if (lane == 2) S.pz[f] = nz;
-            else if (lane == 3) S.pd[f] = off;
-            else if (lane == 4) S.pn[f] = rn;
-            else if (lane == 5) S.pid[f] = id;
-            else S.psrc[f] = src;
+        // the plane (predicated stores of one lane: no divergent branches)
+        if (lane == 0) {
+            S.px[f] = nx;
+            S.py[f] = ny;
+            S.pz[f] = nz;
+            S.pd[f] = off;
+            S.pn[f] = rn;
+            S.pid[f] = id;
+            S.psrc[f] = src;
         }
         if (f >= C.np) C.np = f + 1;
         __syncwarp();
@@ -677,7 +695,13 @@ __device__ __forceinline__ T live_r2(const CellRegs<T, K>& C, int lane) {
             r2 = max(r2, q);
         }
     }
-    return warp_max_t(r2);
+    if constexpr (sizeof(T) == 4) {
+        // r2 >= 0 and never NaN (max drops NaN): its bits order like its
+        // value, so one warp reduction of the bits gives the maximum
+        return __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(r2)));
+    } else {
+        return warp_max_t(r2);
+    }
 }
 
 __device__ __forceinline__ void ring_offset(int s, uint32_t r, int& i, int& j, int& k) {
@@ -795,9 +819,10 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         const int n0 = lane ^ flip(t2), n1 = lane ^ flip(t0), n2 = lane ^ flip(t1);
         S.adj[lane] = (uint32_t)n0 | ((uint32_t)n1 << 8) | ((uint32_t)n2 << 16);
     }
+    C.gen = 0;
     for (int i = lane; i < S_t::P; i += 32) {
-        S.mapf[i] = 0xFF;
-        S.maps[i] = 0xFF;
+        S.mapf[i] = 0xFFFF;
+        S.maps[i] = 0xFFFF;
     }
     // free-slot stack: slots 8 .. VUSE-1, lowest on top
     C.nfree = S_t::VUSE - 8;
