@@ -86,16 +86,48 @@ __global__ void __launch_bounds__(kCsrThreads) k_csr_final(const uint32_t* cnt, 
     if (blockIdx.x == 0 && threadIdx.x == 0) offs[n] = sums[gridDim.x];
 }
 
-__global__ void k_csr_gather(const uint32_t* cnt, const uint64_t* fstart, const int32_t* fnbr,
-                             const double* farea, uint32_t n, const uint64_t* offs, int32_t* nbr,
-                             double* area) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint64_t src = fstart[i], dst = offs[i];
-    const uint32_t c = cnt[i];
-    for (uint32_t t = 0; t < c; ++t) {
-        if (nbr) nbr[dst + t] = fnbr[src + t];
-        if (area) area[dst + t] = farea[src + t];
+// One warp per 32 consecutive cells: their CSR range is contiguous, so the
+// warp writes it as one coalesced stream; each output element finds its cell
+// (lane) by a binary search over the warp's prefix sums of the face counts
+// and reads from that cell's contiguous run in the face pool.
+__global__ void __launch_bounds__(256) k_csr_gather(const uint32_t* cnt, const uint64_t* fstart,
+                                                    const int32_t* fnbr, const double* farea, uint32_t n,
+                                                    const uint64_t* offs, int32_t* nbr, double* area) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint64_t c0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ull;
+    if (c0 >= n) return;                          // whole warps leave together
+    const uint64_t i = c0 + lane;
+    uint32_t c = 0;
+    uint64_t src = 0;
+    if (i < n) {
+        c = cnt[i];
+        src = fstart[i];
+    }
+    const uint64_t dst0 = offs[c0];
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const uint32_t tot = __shfl_sync(kFull, incl, 31);
+    const uint32_t excl = incl - c;
+    for (uint32_t o = 0; o < tot; o += 32) {
+        const uint32_t t = o + lane;
+        int L = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const uint32_t v = __shfl_sync(kFull, incl, L + step - 1);
+            if (v <= t) L += step;
+        }
+        const uint32_t ex = __shfl_sync(kFull, excl, L);
+        const uint64_t sb = __shfl_sync(kFull, src, L);
+        if (t < tot) {
+            const uint64_t k = sb + (t - ex);
+            if (nbr) nbr[dst0 + t] = fnbr[k];
+            if (area) area[dst0 + t] = farea[k];
+        }
     }
 }
 
