@@ -176,7 +176,7 @@ struct Engine {
     uint64_t launches = 0;    // kernels launched so far (all passes)
     cudaGraphExec_t graph = nullptr;
     int graph_precision = -1;
-    int blocks_cache[2][4] = {};
+    int blocks_cache[2][4][2] = {};
 
     ~Engine() { release(); }
 
@@ -197,12 +197,12 @@ struct Engine {
         stream = nullptr;
     }
 
-    int blocks(int precision, int slots) {
+    int blocks(int precision, int slots, bool lean = false) {
         const int si = slots <= 2 ? 0 : (slots <= 4 ? 1 : 2);
-        int& b = blocks_cache[precision][si];
+        int& b = blocks_cache[precision][si][lean ? 1 : 0];
         if (!b) {
             const int wpb = wpb_for(precision, slots);
-            b = clip_blocks_for(precision, slots, wpb, device);
+            b = clip_blocks_for(precision, slots, lean, wpb, device);
         }
         return b;
     }
@@ -446,7 +446,9 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
     base.target_group = group;
     const int s0 = E.cfg.slots_per_lane;
     int cursor = 0;
-    auto pass = [&](int prec, int slots, const uint32_t* work, const unsigned* wcount, uint32_t* l64,
+    // One launch over a work list (null: every cell).  Failed cells append to
+    // the FP64 list (guard, degenerate, verify) and the capacity list.
+    auto pass = [&](int prec, int slots, bool lean, const uint32_t* work, const unsigned* wcount, uint32_t* l64,
                     unsigned* c64, uint32_t* lcap, unsigned* ccap) -> tess_status {
         ClipParams p = base;
         p.work = work;
@@ -459,36 +461,40 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         p.fail_count = cnt + L_FAIL;
         p.reasons = cnt + L_REASON;
         p.work_ctr = (E.cfg.flags & TESS_FLAG_COUNTERS) ? E.d_work : nullptr;
-        CU(launch_clip(p, prec, slots, E.wpb_for(prec, slots), E.blocks(prec, slots), E.stream));
+        CU(launch_clip(p, prec, slots, lean, E.wpb_for(prec, slots), E.blocks(prec, slots, lean), E.stream));
         E.launches += 1;
         return TESS_OK;
     };
+    uint32_t* const* L = E.d_list;
+    // The FP32 first pass over every cell uses the lean form (2 slots per
+    // lane); every other pass carries the window pre-test, which also pays in
+    // the plain FP64 first pass (its serial plane tests run on the slow FP64
+    // pipe).
+    const bool lean = s0 <= 2 && precision == TESS_PRECISION_FP32_GUARD;
     if (timing) CU(cudaEventRecord(ev[0], E.stream));
     if (precision == TESS_PRECISION_FP32_GUARD) {
         // FP32: s0 -> larger capacities; guard / degenerate cells -> FP64 list
         const bool two = s0 < 4, one = s0 < 8;
-        TRY(pass(1, s0, nullptr, nullptr, E.d_list[L_FP64], cnt + L_FP64, one ? E.d_list[L_CAP1] : nullptr,
-                 cnt + L_CAP1));
+        TRY(pass(1, s0, lean, nullptr, nullptr, L[L_FP64], cnt + L_FP64, one ? L[L_CAP1] : nullptr, cnt + L_CAP1));
         if (timing) CU(cudaEventRecord(ev[1], E.stream));
         if (one) {
             const int s1 = two ? 4 : 8;
-            TRY(pass(1, s1, E.d_list[L_CAP1], cnt + L_CAP1, E.d_list[L_FP64], cnt + L_FP64,
-                     two ? E.d_list[L_CAP2] : nullptr, cnt + L_CAP2));
-            if (two)
-                TRY(pass(1, 8, E.d_list[L_CAP2], cnt + L_CAP2, E.d_list[L_FP64], cnt + L_FP64, nullptr, nullptr));
+            TRY(pass(1, s1, false, L[L_CAP1], cnt + L_CAP1, L[L_FP64], cnt + L_FP64, two ? L[L_CAP2] : nullptr,
+                     cnt + L_CAP2));
+            if (two) TRY(pass(1, 8, false, L[L_CAP2], cnt + L_CAP2, L[L_FP64], cnt + L_FP64, nullptr, nullptr));
         }
-        TRY(pass(0, 2, E.d_list[L_FP64], cnt + L_FP64, nullptr, nullptr, E.d_list[L_CAP64A], cnt + L_CAP64A));
-        TRY(pass(0, 4, E.d_list[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, E.d_list[L_CAP64B], cnt + L_CAP64B));
-        TRY(pass(0, 8, E.d_list[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
+        TRY(pass(0, 2, false, L[L_FP64], cnt + L_FP64, nullptr, nullptr, L[L_CAP64A], cnt + L_CAP64A));
+        TRY(pass(0, 4, false, L[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, L[L_CAP64B], cnt + L_CAP64B));
+        TRY(pass(0, 8, false, L[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
     } else {
         const bool two = s0 < 4, one = s0 < 8;
-        TRY(pass(0, s0, nullptr, nullptr, nullptr, nullptr, one ? E.d_list[L_CAP64A] : nullptr, cnt + L_CAP64A));
+        TRY(pass(0, s0, lean, nullptr, nullptr, nullptr, nullptr, one ? L[L_CAP64A] : nullptr, cnt + L_CAP64A));
         if (timing) CU(cudaEventRecord(ev[1], E.stream));
         if (one) {
             const int s1 = two ? 4 : 8;
-            TRY(pass(0, s1, E.d_list[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, two ? E.d_list[L_CAP64B] : nullptr,
+            TRY(pass(0, s1, false, L[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, two ? L[L_CAP64B] : nullptr,
                      cnt + L_CAP64B));
-            if (two) TRY(pass(0, 8, E.d_list[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
+            if (two) TRY(pass(0, 8, false, L[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
         }
     }
     if (timing) CU(cudaEventRecord(ev[2], E.stream));
@@ -646,7 +652,7 @@ tess_status engine_geo(Engine& E, int precision, uint32_t gs, const double* poin
                 p.box[3 + a] = hi[a];
             }
         }
-        CU(launch_clip(p, prec == TESS_PRECISION_FP32_GUARD ? 1 : 0, 8, 1, 1, E.stream));
+        CU(launch_clip(p, prec == TESS_PRECISION_FP32_GUARD ? 1 : 0, 8, false, 1, 1, E.stream));
         CU(cudaMemcpyAsync(out, E.d_geo, sizeof(GeoOut), cudaMemcpyDeviceToHost, E.stream));
         CU(cudaStreamSynchronize(E.stream));
         if (out->status == ST_OK) return TESS_OK;

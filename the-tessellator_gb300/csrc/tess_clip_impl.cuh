@@ -57,6 +57,11 @@ constexpr bool kBatch2 = false;
 // Load the next batch's table entries and bin ranges before cutting the
 // current batch (overlaps their latency, costs registers).
 constexpr bool kPrefetch = true;
+// Pre-test a window's candidates against the live vertices (re-run form)
+// when at least this many are within twice the cell radius.  The lean
+// first-pass form leaves it out: on uniform inputs windows are small and its
+// mere presence costs the hot loop registers.
+constexpr int kPretestMin = 2;
 
 template <typename T, int K>
 struct Smem {
@@ -727,7 +732,7 @@ __device__ __forceinline__ void ring_offset(int s, uint32_t r, int& i, int& j, i
     }
 }
 
-template <typename T, int K, bool GEO>
+template <typename T, int K, bool GEO, bool LEAN>
 __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int lane, Work& W) {
     using S_t = Smem<T, K>;
     constexpr bool GUARD = sizeof(T) == 4;
@@ -890,6 +895,33 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 if (keep && tgroup >= 0) keep = (int64_t)(P.sgroup ? P.sgroup[j] : 0u) == tgroup;
             }
             unsigned km = __ballot_sync(FULL, keep);
+            // Pre-test the window at once: each lane tests its own candidate's
+            // bisector against every live vertex (read from the shared
+            // mirror).  A bisector with no vertex Outside cuts nothing now and
+            // nothing later (the cell only shrinks), so only possible cutters
+            // (and guard-band cases, which the serial test reports) go on to
+            // the serial nearest-first loop.  Same arithmetic as cut().
+            if (!LEAN && __popc(km) >= kPretestMin) {
+                bool maycut = false;
+                if (keep) {
+                    T nx_, ny_, nz_, off_, rn_;
+                    bisector(rx, ry, rz, r2, nx_, ny_, nz_, off_, rn_);
+                    bool out = false, amb = false;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        uint32_t m = C.lm[k];
+                        while (m) {
+                            const int sl = k * 32 + __ffs(m) - 1;
+                            m &= m - 1u;
+                            const T sd = sdist(nx_, ny_, nz_, off_, S.vx[sl], S.vy[sl], S.vz[sl]);
+                            out |= sd > (GUARD ? (T)0 : (T)kTolerance);
+                            if constexpr (GUARD) amb |= fabs(sd) <= rn_ * (S.ve[sl] + cR);
+                        }
+                    }
+                    maycut = out || amb;
+                }
+                km = __ballot_sync(FULL, keep && maycut);
+            }
             // Nearest first: repeatedly take the closest remaining candidate
             // (warp minimum of its distance, ties by lane), so the closest
             // bisectors shrink the cell before the farther ones are tested.
@@ -1377,7 +1409,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
 }
 
 // K = 2: 8 warps per block, two blocks per SM (registers capped at 128).
-template <typename T, int K, bool GEO>
+template <typename T, int K, bool GEO, bool LEAN>
 __global__ void __launch_bounds__(K == 2 ? 256 : 128, K == 2 ? 2 : 1) k_clip(ClipParams P) {
     extern __shared__ __align__(16) unsigned char smraw[];
     Smem<T, K>& S = reinterpret_cast<Smem<T, K>*>(smraw)[threadIdx.x >> 5];
@@ -1390,7 +1422,7 @@ __global__ void __launch_bounds__(K == 2 ? 256 : 128, K == 2 ? 2 : 1) k_clip(Cli
         const unsigned total = P.work_count ? *P.work_count : P.total;
         if (w >= total) break;
         const uint32_t gs = P.work ? P.work[w] : w;
-        run_cell<T, K, GEO>(P, S, gs, lane, W);
+        run_cell<T, K, GEO, LEAN>(P, S, gs, lane, W);
     }
     if (P.work_ctr && lane == 0) {
         atomicAdd(&P.work_ctr[0], (unsigned long long)W.tested);
@@ -1403,30 +1435,30 @@ __global__ void __launch_bounds__(K == 2 ? 256 : 128, K == 2 ? 2 : 1) k_clip(Cli
 
 // Raise the kernel's dynamic shared memory limit to what `bytes` needs (once
 // per size); kept out of stream capture by the host's warm-up calls.
-template <typename T, int K, bool GEO>
+template <typename T, int K, bool GEO, bool LEAN>
 cudaError_t configure_smem(size_t bytes) {
     static size_t configured = 0;
     if (bytes <= configured) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_clip<T, K, GEO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaError_t e = cudaFuncSetAttribute(k_clip<T, K, GEO, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) configured = bytes;
     return e;
 }
 
-template <typename T, int K, bool GEO>
+template <typename T, int K, bool GEO, bool LEAN>
 cudaError_t launch_t(const ClipParams& p, int wpb, int blocks, cudaStream_t s) {
     const size_t sm = sizeof(Smem<T, K>) * (size_t)wpb;
-    cudaError_t e = configure_smem<T, K, GEO>(sm);
+    cudaError_t e = configure_smem<T, K, GEO, LEAN>(sm);
     if (e != cudaSuccess) return e;
-    k_clip<T, K, GEO><<<blocks, 32 * wpb, sm, s>>>(p);
+    k_clip<T, K, GEO, LEAN><<<blocks, 32 * wpb, sm, s>>>(p);
     return cudaGetLastError();
 }
 
-template <typename T, int K, bool GEO>
+template <typename T, int K, bool GEO, bool LEAN>
 int blocks_t(int wpb, int device) {
     const size_t sm = sizeof(Smem<T, K>) * (size_t)wpb;
     int per = 0, nsm = 0;
-    if (configure_smem<T, K, GEO>(sm) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_clip<T, K, GEO>, 32 * wpb, sm) != cudaSuccess)
+    if (configure_smem<T, K, GEO, LEAN>(sm) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_clip<T, K, GEO, LEAN>, 32 * wpb, sm) != cudaSuccess)
         per = 1;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
     cudaGetLastError();   // leave no sticky error behind a failed query
