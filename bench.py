@@ -47,6 +47,14 @@ WORKLOADS = {
 }
 RADIUS_METRIC = "radius queries/sec on 1 GB300 (find_neighbors_in_real_radius, FP64, exact)"
 
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
+# captures of the same kernels on GB300.  The clipping pass was captured at
+# 1,000,000 cells (75.5 MB read + 169.6 MB written) and is scaled by cells: its
+# traffic is its output plus L2 misses, both per cell.  The radius passes were
+# captured at full size (16,777,216 queries, radius 0.006).
+NCU_CLIP_BYTES_PER_CELL = (75.547648e6 + 169.617408e6) / 1_000_000
+NCU_RADIUS_BYTES = {"count": 3.846207488e9 + 0.50285184e9, "fill": 6.337812736e9 + 1.53743616e9}
+
 
 def make_points(name, points=None):
     from tessellator import workloads as W
@@ -341,8 +349,10 @@ def run_ours(args, ws, rank, local):
         if batched is None:
             achieved = fpc * n / (np.mean(clip_ms) / 1e3) / 1e12
             out["roofline"] = {
-                "kernel": "k_clip<float,2> (first clipping pass)", "bound": "fp32", "achieved": achieved,
-                "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32, "traffic": None,
+                "kernel": "k_clip<float,2,lean> (first clipping pass)", "bound": "fp32", "achieved": achieved,
+                "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32,
+                "traffic": NCU_CLIP_BYTES_PER_CELL * n,
+                "traffic_source": "ncu DRAM bytes at 1,000,000 cells, scaled by cells",
                 "flops_per_cell": fpc,
                 "peak_source": f"nominal: {nsm} SMs x 128 FP32 lanes x 2 x {sm_mhz:.0f} MHz (sampled SM clock)",
             }
@@ -466,9 +476,9 @@ def run_radius(args, ws, rank, local):
     bytes_count = (24 + 24 + 4) * n
     bytes_fill = (24 + 24 + 8) * n + 4 * total
     if f_ms >= c_ms:
-        kname, kbytes, kms = "k_radius<REAL_RADIUS, fill>", bytes_fill, f_ms
+        kname, kbytes, kms, kkey = "k_radius<REAL_RADIUS, fill>", bytes_fill, f_ms, "fill"
     else:
-        kname, kbytes, kms = "k_radius<REAL_RADIUS, count> + offsets scan", bytes_count, c_ms
+        kname, kbytes, kms, kkey = "k_radius<REAL_RADIUS, count> + offsets scan", bytes_count, c_ms, "count"
     ach = kbytes / (kms / 1e3) / 1e9
     out = {
         "metric": RADIUS_METRIC, "value": n * ws / (ms / 1e3), "unit": "queries/s", "n_gpus": ws,
@@ -482,7 +492,10 @@ def run_radius(args, ws, rank, local):
         "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
         "passes_ms": {"count_and_scan": c_ms, "fill": f_ms},
         "roofline": {"kernel": kname, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-                     "frac": ach / hbm, "traffic": None, "algorithmic_bytes": kbytes, "peak_source": src},
+                     "frac": ach / hbm,
+                     "traffic": NCU_RADIUS_BYTES[kkey] if n == w["n"] else None,
+                     "traffic_source": "ncu DRAM bytes of the same launch at 16,777,216 queries",
+                     "algorithmic_bytes": kbytes, "peak_source": src},
     }
     if rank == 0 and not args.no_cpu_baseline:
         rate, desc = radius_cpu_baseline(pts, radius, min(args.cpu_seconds, 10.0))
