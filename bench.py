@@ -333,7 +333,8 @@ def run_ours(args, ws, rank, local):
         "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
         "passes_ms": {"grid": float(np.mean(grid_ms)), "clip_first_pass": float(np.mean(clip_ms)),
                       "reruns": float(np.mean(rerun_ms)), "csr": float(np.mean(csr_ms))},
-        "reruns": {"fp64": int(st1["rerun_fp64"]), "capacity": int(st1["rerun_capacity"]),
+        "reruns": {"fp32_hybrid": int(st1["rerun_fp64"]), "fp64_full": int(st1["rerun_fp64_full"]),
+                   "capacity": int(st1["rerun_capacity"]),
                    "failed": int(st1["failed"]), "guard": int(st1["rerun_guard"]),
                    "verify": int(st1["rerun_verify"]), "degenerate": int(st1["rerun_degenerate"])},
     }

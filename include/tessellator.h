@@ -109,6 +109,9 @@ typedef struct {
      * pass (with the scan of the counts) and of its fill pass. */
     double ms_query_count;
     double ms_query_fill;
+    /* FP32 form: of the rerun_fp64 cells, those the hybrid re-run (guard-band
+     * tests decided in FP64) could not settle, re-run entirely in FP64 */
+    uint64_t rerun_fp64_full;
 } tess_stats;
 
 void tess_config_default(tess_config* cfg);

@@ -66,7 +66,11 @@ int64_t cells_per_dim(uint64_t n, double density) {
     return (int64_t)v + 1;
 }
 
-enum { L_FP64 = 0, L_CAP1 = 1, L_CAP2 = 2, L_CAP64A = 3, L_CAP64B = 4, L_COUNT = 5, L_FAIL = 6, L_REASON = 8 };
+// Work lists of the re-run passes: FP64 (cells the FP32 passes flagged),
+// CAP1/CAP2 (FP32 capacity), CAP64A/B (FP64 capacity), FP64B (cells the
+// hybrid FP32 pass could not settle).
+enum { L_FP64 = 0, L_CAP1 = 1, L_CAP2 = 2, L_CAP64A = 3, L_CAP64B = 4, L_FP64B = 5, L_COUNT = 6, L_FAIL = 6,
+       L_REASON = 8 };
 // Kernels launched by one binning pass (launch_grid_build).
 constexpr uint64_t kGridLaunches = 11;
 
@@ -176,7 +180,7 @@ struct Engine {
     uint64_t launches = 0;    // kernels launched so far (all passes)
     cudaGraphExec_t graph = nullptr;
     int graph_precision = -1;
-    int blocks_cache[2][4][2] = {};
+    int blocks_cache[2][4][3] = {};
 
     ~Engine() { release(); }
 
@@ -197,12 +201,12 @@ struct Engine {
         stream = nullptr;
     }
 
-    int blocks(int precision, int slots, bool lean = false) {
+    int blocks(int precision, int slots, int form = kFormStd) {
         const int si = slots <= 2 ? 0 : (slots <= 4 ? 1 : 2);
-        int& b = blocks_cache[precision][si][lean ? 1 : 0];
+        int& b = blocks_cache[precision][si][form];
         if (!b) {
             const int wpb = wpb_for(precision, slots);
-            b = clip_blocks_for(precision, slots, lean, wpb, device);
+            b = clip_blocks_for(precision, slots, form, wpb, device);
         }
         return b;
     }
@@ -448,7 +452,7 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
     int cursor = 0;
     // One launch over a work list (null: every cell).  Failed cells append to
     // the FP64 list (guard, degenerate, verify) and the capacity list.
-    auto pass = [&](int prec, int slots, bool lean, const uint32_t* work, const unsigned* wcount, uint32_t* l64,
+    auto pass = [&](int prec, int slots, int form, const uint32_t* work, const unsigned* wcount, uint32_t* l64,
                     unsigned* c64, uint32_t* lcap, unsigned* ccap) -> tess_status {
         ClipParams p = base;
         p.work = work;
@@ -461,40 +465,40 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         p.fail_count = cnt + L_FAIL;
         p.reasons = cnt + L_REASON;
         p.work_ctr = (E.cfg.flags & TESS_FLAG_COUNTERS) ? E.d_work : nullptr;
-        CU(launch_clip(p, prec, slots, lean, E.wpb_for(prec, slots), E.blocks(prec, slots, lean), E.stream));
+        CU(launch_clip(p, prec, slots, form, E.wpb_for(prec, slots), E.blocks(prec, slots, form), E.stream));
         E.launches += 1;
         return TESS_OK;
     };
     uint32_t* const* L = E.d_list;
-    // The FP32 first pass over every cell uses the lean form (2 slots per
-    // lane); every other pass carries the window pre-test, which also pays in
-    // the plain FP64 first pass (its serial plane tests run on the slow FP64
-    // pipe).
-    const bool lean = s0 <= 2 && precision == TESS_PRECISION_FP32_GUARD;
     if (timing) CU(cudaEventRecord(ev[0], E.stream));
     if (precision == TESS_PRECISION_FP32_GUARD) {
-        // FP32: s0 -> larger capacities; guard / degenerate cells -> FP64 list
+        // FP32: the lean first pass (2 slots per lane) over every cell;
+        // capacity re-runs at 4 and 8 slots; the flagged cells re-run in the
+        // hybrid form (guard-band tests decided in FP64); what that cannot
+        // settle runs in the FP64 form.
         const bool two = s0 < 4, one = s0 < 8;
-        TRY(pass(1, s0, lean, nullptr, nullptr, L[L_FP64], cnt + L_FP64, one ? L[L_CAP1] : nullptr, cnt + L_CAP1));
+        TRY(pass(1, s0, s0 <= 2 ? kFormLean : kFormStd, nullptr, nullptr, L[L_FP64], cnt + L_FP64,
+                 one ? L[L_CAP1] : nullptr, cnt + L_CAP1));
         if (timing) CU(cudaEventRecord(ev[1], E.stream));
         if (one) {
             const int s1 = two ? 4 : 8;
-            TRY(pass(1, s1, false, L[L_CAP1], cnt + L_CAP1, L[L_FP64], cnt + L_FP64, two ? L[L_CAP2] : nullptr,
+            TRY(pass(1, s1, kFormStd, L[L_CAP1], cnt + L_CAP1, L[L_FP64], cnt + L_FP64, two ? L[L_CAP2] : nullptr,
                      cnt + L_CAP2));
-            if (two) TRY(pass(1, 8, false, L[L_CAP2], cnt + L_CAP2, L[L_FP64], cnt + L_FP64, nullptr, nullptr));
+            if (two) TRY(pass(1, 8, kFormStd, L[L_CAP2], cnt + L_CAP2, L[L_FP64], cnt + L_FP64, nullptr, nullptr));
         }
-        TRY(pass(0, 2, false, L[L_FP64], cnt + L_FP64, nullptr, nullptr, L[L_CAP64A], cnt + L_CAP64A));
-        TRY(pass(0, 4, false, L[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, L[L_CAP64B], cnt + L_CAP64B));
-        TRY(pass(0, 8, false, L[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
+        TRY(pass(1, 2, kFormHybrid, L[L_FP64], cnt + L_FP64, L[L_FP64B], cnt + L_FP64B, L[L_FP64B], cnt + L_FP64B));
+        TRY(pass(0, 2, kFormStd, L[L_FP64B], cnt + L_FP64B, nullptr, nullptr, L[L_CAP64A], cnt + L_CAP64A));
+        TRY(pass(0, 4, kFormStd, L[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, L[L_CAP64B], cnt + L_CAP64B));
+        TRY(pass(0, 8, kFormStd, L[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
     } else {
         const bool two = s0 < 4, one = s0 < 8;
-        TRY(pass(0, s0, lean, nullptr, nullptr, nullptr, nullptr, one ? L[L_CAP64A] : nullptr, cnt + L_CAP64A));
+        TRY(pass(0, s0, kFormStd, nullptr, nullptr, nullptr, nullptr, one ? L[L_CAP64A] : nullptr, cnt + L_CAP64A));
         if (timing) CU(cudaEventRecord(ev[1], E.stream));
         if (one) {
             const int s1 = two ? 4 : 8;
-            TRY(pass(0, s1, false, L[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, two ? L[L_CAP64B] : nullptr,
+            TRY(pass(0, s1, kFormStd, L[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, two ? L[L_CAP64B] : nullptr,
                      cnt + L_CAP64B));
-            if (two) TRY(pass(0, 8, false, L[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
+            if (two) TRY(pass(0, 8, kFormStd, L[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
         }
     }
     if (timing) CU(cudaEventRecord(ev[2], E.stream));
@@ -538,9 +542,11 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
         E.stats.faces = used;
         if (precision == TESS_PRECISION_FP32_GUARD) {
             E.stats.rerun_fp64 = counts[L_FP64];
+            E.stats.rerun_fp64_full = counts[L_FP64B];
             E.stats.rerun_capacity = (uint64_t)counts[L_CAP1] + counts[L_CAP2] + counts[L_CAP64A] + counts[L_CAP64B];
         } else {
             E.stats.rerun_fp64 = 0;
+            E.stats.rerun_fp64_full = 0;
             E.stats.rerun_capacity = (uint64_t)counts[L_CAP64A] + counts[L_CAP64B];
         }
         if (E.ndiag == 1) {
@@ -652,7 +658,7 @@ tess_status engine_geo(Engine& E, int precision, uint32_t gs, const double* poin
                 p.box[3 + a] = hi[a];
             }
         }
-        CU(launch_clip(p, prec == TESS_PRECISION_FP32_GUARD ? 1 : 0, 8, false, 1, 1, E.stream));
+        CU(launch_clip(p, prec == TESS_PRECISION_FP32_GUARD ? 1 : 0, 8, kFormStd, 1, 1, E.stream));
         CU(cudaMemcpyAsync(out, E.d_geo, sizeof(GeoOut), cudaMemcpyDeviceToHost, E.stream));
         CU(cudaStreamSynchronize(E.stream));
         if (out->status == ST_OK) return TESS_OK;
@@ -1353,6 +1359,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
     E.stats.cells = E.total;
     E.stats.faces = used;
     E.stats.rerun_fp64 = prec == 1 ? counts[L_FP64] : 0;
+    E.stats.rerun_fp64_full = prec == 1 ? counts[L_FP64B] : 0;
     E.stats.rerun_capacity = (uint64_t)counts[L_CAP1] + counts[L_CAP2] + counts[L_CAP64A] + counts[L_CAP64B];
     E.stats.failed = counts[L_FAIL];
     E.stats.rerun_guard = counts[L_REASON + ST_GUARD];

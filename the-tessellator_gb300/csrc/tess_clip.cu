@@ -133,14 +133,14 @@ __global__ void __launch_bounds__(256) k_csr_gather(const uint32_t* cnt, const u
 
 }  // namespace
 
-cudaError_t launch_clip(const ClipParams& p, int precision, int slots, bool lean, int wpb, int blocks,
+cudaError_t launch_clip(const ClipParams& p, int precision, int slots, int form, int wpb, int blocks,
                         cudaStream_t s) {
-    return precision == 1 ? launch_clip_f32(p, slots, lean, wpb, blocks, s)
-                          : launch_clip_f64(p, slots, lean, wpb, blocks, s);
+    return precision == 1 ? launch_clip_f32(p, slots, form, wpb, blocks, s)
+                          : launch_clip_f64(p, slots, form, wpb, blocks, s);
 }
 
-int clip_blocks_for(int precision, int slots, bool lean, int wpb, int device) {
-    return precision == 1 ? clip_blocks_f32(slots, lean, wpb, device) : clip_blocks_f64(slots, lean, wpb, device);
+int clip_blocks_for(int precision, int slots, int form, int wpb, int device) {
+    return precision == 1 ? clip_blocks_f32(slots, form, wpb, device) : clip_blocks_f64(slots, form, wpb, device);
 }
 
 size_t csr_tmp_words(uint32_t n) {

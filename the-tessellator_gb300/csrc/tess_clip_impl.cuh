@@ -274,7 +274,7 @@ struct Regs {
     T v[K];
 };
 
-template <typename T, int K, bool GUARD>
+template <typename T, int K, bool GUARD, bool RESOLVE>
 __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, const Regs<T, K> sdv,
                                         const Regs<uint32_t, K> omv, T nx, T ny, T nz, T off, T rn, T cR,
                                         int32_t id, uint32_t src, int f, int lane) {
@@ -365,6 +365,7 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
 #pragma unroll
     for (int k = 0; k < K; ++k) newm[k] = 0;
     bool bad = false;
+    bool numbad = false;
     for (int r0 = 0; r0 < B; r0 += 32) {
         const int qi = r0 + lane;
         const bool act = qi < B;
@@ -401,6 +402,10 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
                 // e = kVertexErr |x|_1 / dhat, dhat = |det| / (|n_a| |n_b| |n_f|)
                 pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) * (S.pn[a] * S.pn[b] * rn) * fabs(inv);
                 if (!(pe < (T)1e30)) pe = (T)1e30;
+                // hybrid form: a cell that keeps going after FP64-decided
+                // tests must not carry an ill-conditioned (or non-finite)
+                // FP32 vertex; it re-runs in FP64 instead
+                if (RESOLVE && !(pe <= (T)1000 * cR)) numbad = true;
             } else {
                 const T den = xsd - ysd;
                 const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / den;
@@ -410,6 +415,7 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
             }
             slot = select_k<K>(fm, qi);
         }
+        if (RESOLVE && __any_sync(FULL, numbad)) return -ST_GUARD;
         __syncwarp();
         if (act) {
             S.vx[slot] = px;
@@ -503,9 +509,64 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
 //     cannot be decided in FP32: the cell goes to the FP64 form (ST_GUARD).
 // Returns 1 when vertices were cut off, 0 when nothing was Outside, or
 // -status.
-template <typename T, int K, bool GUARD>
+// FP64 view of the site and its container, for deciding guard-band plane
+// tests in FP64 (hybrid form).
+struct Fp64Site {
+    double sx, sy, sz;
+    const double* blo;
+    const double* bhi;
+};
+
+// Side of the vertex in slot s relative to the bisector of the site and the
+// point at sorted position cj, decided in FP64: the vertex is recomputed from
+// its three planes (walls, or bisectors of the site and the FP64 points that
+// made them) by Cramer's rule, and classified with the reference's test on
+// the normalised bisector (vector3.rs:170-239, tolerance 1e-12).  Returns 1
+// (Outside), -1 (Inside or Incident) or 0 (the three planes are singular).
+template <typename T, int K>
+__device__ __noinline__ int resolve_fp64(const Smem<T, K>& S, const ClipParams& P, const Fp64Site& st, int s,
+                                         uint32_t cj) {
+    const uint32_t tt = S.tri[s];
+    double n[3][3], h[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const int p = plane_of(tt, e);
+        if (p < 6) {
+            const int a = p >> 1;
+            const bool mx = p & 1;
+            const double s_a = a == 0 ? st.sx : (a == 1 ? st.sy : st.sz);
+            n[e][0] = a == 0 ? (mx ? 1.0 : -1.0) : 0.0;
+            n[e][1] = a == 1 ? (mx ? 1.0 : -1.0) : 0.0;
+            n[e][2] = a == 2 ? (mx ? 1.0 : -1.0) : 0.0;
+            h[e] = mx ? (st.bhi[a] - s_a) : (s_a - st.blo[a]);
+        } else {
+            const uint32_t j = S.psrc[p];
+            n[e][0] = P.spx[j] - st.sx;
+            n[e][1] = P.spy[j] - st.sy;
+            n[e][2] = P.spz[j] - st.sz;
+            h[e] = 0.5 * (n[e][0] * n[e][0] + n[e][1] * n[e][1] + n[e][2] * n[e][2]);
+        }
+    }
+    const double bc0 = n[1][1] * n[2][2] - n[1][2] * n[2][1], bc1 = n[1][2] * n[2][0] - n[1][0] * n[2][2],
+                 bc2 = n[1][0] * n[2][1] - n[1][1] * n[2][0];
+    const double ca0 = n[2][1] * n[0][2] - n[2][2] * n[0][1], ca1 = n[2][2] * n[0][0] - n[2][0] * n[0][2],
+                 ca2 = n[2][0] * n[0][1] - n[2][1] * n[0][0];
+    const double ab0 = n[0][1] * n[1][2] - n[0][2] * n[1][1], ab1 = n[0][2] * n[1][0] - n[0][0] * n[1][2],
+                 ab2 = n[0][0] * n[1][1] - n[0][1] * n[1][0];
+    const double det = n[0][0] * bc0 + n[0][1] * bc1 + n[0][2] * bc2;
+    if (!(fabs(det) > 0.0)) return 0;
+    const double x = (h[0] * bc0 + h[1] * ca0 + h[2] * ab0) / det;
+    const double y = (h[0] * bc1 + h[1] * ca1 + h[2] * ab1) / det;
+    const double z = (h[0] * bc2 + h[1] * ca2 + h[2] * ab2) / det;
+    const double qx = P.spx[cj] - st.sx, qy = P.spy[cj] - st.sy, qz = P.spz[cj] - st.sz;
+    const double q2 = qx * qx + qy * qy + qz * qz;
+    const double sd = (qx * x + qy * y + qz * z - 0.5 * q2) / sqrt(q2);
+    return sd > kTolerance ? 1 : -1;
+}
+
+template <typename T, int K, bool GUARD, bool RESOLVE = false>
 __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T rn, T cR, int32_t id,
-                   uint32_t src, int lane) {
+                   uint32_t src, int lane, const ClipParams& P, const Fp64Site& site) {
     using S_t = Smem<T, K>;
     T sd[K];
     uint32_t om[K];
@@ -524,7 +585,29 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         if constexpr (GUARD) gh |= live && fabs(sd[k]) <= rn * (C.ve[k] + cR);
         om[k] = __ballot_sync(FULL, out);
     }
-    if (GUARD && __any_sync(FULL, gh)) return -ST_GUARD;
+    if (GUARD && __any_sync(FULL, gh)) {
+        if constexpr (!RESOLVE) {
+            return -ST_GUARD;
+        } else {
+            // decide the guard-band vertices in FP64 (src is the candidate's
+            // sorted index); the rest keep their FP32 decision
+            bool fail = false;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (C.lm[k] == 0) continue;
+                const bool live = (C.lm[k] >> lane) & 1u;
+                const bool amb = live && fabs(sd[k]) <= rn * (C.ve[k] + cR);
+                bool out = live && sd[k] > (T)0;
+                if (amb) {
+                    const int r = resolve_fp64<T, K>(S, P, site, k * 32 + lane, src);
+                    fail |= r == 0;
+                    out = r > 0;
+                }
+                om[k] = __ballot_sync(FULL, out);
+            }
+            if (__any_sync(FULL, fail)) return -ST_GUARD;
+        }
+    }
     uint32_t anyo = 0;
 #pragma unroll
     for (int k = 0; k < K; ++k) anyo |= om[k];
@@ -591,6 +674,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         int slot = 0;
         uint32_t ty = 0;
         T px = 0, py = 0, pz = 0, pe = 0;
+        bool numbad = false;
         if (bnd) {
             if constexpr (GUARD) {
                 // the vertex of planes (a, b, f) by Cramer's rule (see above)
@@ -607,6 +691,10 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
                 // e = kVertexErr |x|_1 / dhat, dhat = |det| / (|n_a| |n_b| |n_f|)
                 pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) * (S.pn[a] * S.pn[b] * rn) * fabs(inv);
                 if (!(pe < (T)1e30)) pe = (T)1e30;
+                // hybrid form: a cell that keeps going after FP64-decided
+                // tests must not carry an ill-conditioned (or non-finite)
+                // FP32 vertex; it re-runs in FP64 instead
+                if (RESOLVE && !(pe <= (T)1000 * cR)) numbad = true;
             } else {
                 const T xx = S.vx[x], xy = S.vy[x], xz = S.vz[x], xsd = S.vsd[x];
                 const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
@@ -618,6 +706,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             ty = S.tri[y];
             slot = S.fl[base + R - 1 - q];
         }
+        if (RESOLVE && __any_sync(FULL, numbad)) return -ST_GUARD;
         __syncwarp();
         if (bnd) {
             S.vx[slot] = px;
@@ -680,7 +769,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         sdv.v[k] = sd[k];
         omv.v[k] = om[k];
     }
-    return cut_general<T, K, GUARD>(S, C, sdv, omv, nx, ny, nz, off, rn, cR, id, src, f, lane);
+    return cut_general<T, K, GUARD, RESOLVE>(S, C, sdv, omv, nx, ny, nz, off, rn, cR, id, src, f, lane);
 }
 
 // Squared radius of the cell about its site: max |v|^2 over live vertices;
@@ -732,7 +821,7 @@ __device__ __forceinline__ void ring_offset(int s, uint32_t r, int& i, int& j, i
     }
 }
 
-template <typename T, int K, bool GEO, bool LEAN>
+template <typename T, int K, bool GEO, int FORM>
 __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int lane, Work& W) {
     using S_t = Smem<T, K>;
     constexpr bool GUARD = sizeof(T) == 4;
@@ -781,6 +870,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     // ---- the container box, translated by -site (polyhedron.rs:268-392) ----
     const double* blo = P.box_override ? P.box : D.blo;
     const double* bhi = P.box_override ? P.box + 3 : D.bhi;
+    const Fp64Site fsite{sx, sy, sz, blo, bhi};
     CellRegs<T, K> C;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -901,7 +991,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             // nothing later (the cell only shrinks), so only possible cutters
             // (and guard-band cases, which the serial test reports) go on to
             // the serial nearest-first loop.  Same arithmetic as cut().
-            if (!LEAN && __popc(km) >= kPretestMin) {
+            if (FORM != kFormLean && __popc(km) >= kPretestMin) {
                 bool maycut = false;
                 if (keep) {
                     T nx_, ny_, nz_, off_, rn_;
@@ -946,14 +1036,21 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 }
                 T nx, ny, nz, off, rn;
                 bisector(cx, cy, cz, c2, nx, ny, nz, off, rn);
-                const int r = cut<T, K, GUARD>(S, C, nx, ny, nz, off, rn, cR, cidb, cj, lane);
+                const int r = cut<T, K, GUARD, FORM == kFormHybrid>(S, C, nx, ny, nz, off, rn, cR, cidb, cj, lane, P,
+                                                                       fsite);
                 ++W.tested;
                 if (r < 0) return -r;
                 if (r > 0) {
                     ++W.cuts;
                     W.newv += (unsigned)(r - 1);
+                    const T R2b = R2;
                     R2 = live_r2(C, lane);
                     cR = (T)P.guard_rel * sqrt_up(R2);
+                    // hybrid form: a cut never moves a vertex beyond the cell
+                    // (convexity), so a radius that grew (or is no longer
+                    // finite) means an FP32 vertex went wrong after an
+                    // FP64-decided test; the cell re-runs in FP64
+                    if (FORM == kFormHybrid && !(R2 <= R2b * (T)1.001)) return ST_GUARD;
                 }
             }
         }
@@ -1409,7 +1506,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
 }
 
 // K = 2: 8 warps per block, two blocks per SM (registers capped at 128).
-template <typename T, int K, bool GEO, bool LEAN>
+template <typename T, int K, bool GEO, int FORM>
 __global__ void __launch_bounds__(K == 2 ? 256 : 128, K == 2 ? 2 : 1) k_clip(ClipParams P) {
     extern __shared__ __align__(16) unsigned char smraw[];
     Smem<T, K>& S = reinterpret_cast<Smem<T, K>*>(smraw)[threadIdx.x >> 5];
@@ -1422,7 +1519,7 @@ __global__ void __launch_bounds__(K == 2 ? 256 : 128, K == 2 ? 2 : 1) k_clip(Cli
         const unsigned total = P.work_count ? *P.work_count : P.total;
         if (w >= total) break;
         const uint32_t gs = P.work ? P.work[w] : w;
-        run_cell<T, K, GEO, LEAN>(P, S, gs, lane, W);
+        run_cell<T, K, GEO, FORM>(P, S, gs, lane, W);
     }
     if (P.work_ctr && lane == 0) {
         atomicAdd(&P.work_ctr[0], (unsigned long long)W.tested);
@@ -1435,30 +1532,30 @@ __global__ void __launch_bounds__(K == 2 ? 256 : 128, K == 2 ? 2 : 1) k_clip(Cli
 
 // Raise the kernel's dynamic shared memory limit to what `bytes` needs (once
 // per size); kept out of stream capture by the host's warm-up calls.
-template <typename T, int K, bool GEO, bool LEAN>
+template <typename T, int K, bool GEO, int FORM>
 cudaError_t configure_smem(size_t bytes) {
     static size_t configured = 0;
     if (bytes <= configured) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_clip<T, K, GEO, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaError_t e = cudaFuncSetAttribute(k_clip<T, K, GEO, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) configured = bytes;
     return e;
 }
 
-template <typename T, int K, bool GEO, bool LEAN>
+template <typename T, int K, bool GEO, int FORM>
 cudaError_t launch_t(const ClipParams& p, int wpb, int blocks, cudaStream_t s) {
     const size_t sm = sizeof(Smem<T, K>) * (size_t)wpb;
-    cudaError_t e = configure_smem<T, K, GEO, LEAN>(sm);
+    cudaError_t e = configure_smem<T, K, GEO, FORM>(sm);
     if (e != cudaSuccess) return e;
-    k_clip<T, K, GEO, LEAN><<<blocks, 32 * wpb, sm, s>>>(p);
+    k_clip<T, K, GEO, FORM><<<blocks, 32 * wpb, sm, s>>>(p);
     return cudaGetLastError();
 }
 
-template <typename T, int K, bool GEO, bool LEAN>
+template <typename T, int K, bool GEO, int FORM>
 int blocks_t(int wpb, int device) {
     const size_t sm = sizeof(Smem<T, K>) * (size_t)wpb;
     int per = 0, nsm = 0;
-    if (configure_smem<T, K, GEO, LEAN>(sm) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_clip<T, K, GEO, LEAN>, 32 * wpb, sm) != cudaSuccess)
+    if (configure_smem<T, K, GEO, FORM>(sm) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_clip<T, K, GEO, FORM>, 32 * wpb, sm) != cudaSuccess)
         per = 1;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
     cudaGetLastError();   // leave no sticky error behind a failed query

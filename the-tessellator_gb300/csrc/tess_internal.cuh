@@ -262,17 +262,24 @@ struct ClipParams {
     double box[6];                // lo xyz, hi xyz
 };
 
-// lean: the first-pass form (2 slots per lane, no window pre-test).  The
-// re-run passes use the form with the pre-test, which cells next to dense
-// clusters (hundreds of candidates) need.
-cudaError_t launch_clip_f32(const ClipParams& p, int slots, bool lean, int wpb, int blocks, cudaStream_t s);
-cudaError_t launch_clip_f64(const ClipParams& p, int slots, bool lean, int wpb, int blocks, cudaStream_t s);
-int clip_blocks_f32(int slots, bool lean, int wpb, int device);
-int clip_blocks_f64(int slots, bool lean, int wpb, int device);
+// Forms of the clipping kernel:
+//   kFormLean    the FP32 first pass (2 slots per lane, no window pre-test);
+//   kFormStd     the re-run passes and the plain FP64 form, with the window
+//                pre-test (cells next to dense clusters test hundreds of
+//                candidates);
+//   kFormHybrid  FP32, 2 slots per lane, with the pre-test, for cells the
+//                first pass flagged: a plane test in the guard band is
+//                decided in FP64 for the vertices concerned (each recomputed
+//                from its three planes) instead of re-running the cell.
+enum ClipForm : int { kFormLean = 0, kFormStd = 1, kFormHybrid = 2 };
+cudaError_t launch_clip_f32(const ClipParams& p, int slots, int form, int wpb, int blocks, cudaStream_t s);
+cudaError_t launch_clip_f64(const ClipParams& p, int slots, int form, int wpb, int blocks, cudaStream_t s);
+int clip_blocks_f32(int slots, int form, int wpb, int device);
+int clip_blocks_f64(int slots, int form, int wpb, int device);
 // precision: 0 FP64, 1 FP32.  slots: 2, 4 or 8.
-cudaError_t launch_clip(const ClipParams& p, int precision, int slots, bool lean, int warps_per_block,
+cudaError_t launch_clip(const ClipParams& p, int precision, int slots, int form, int warps_per_block,
                         int blocks, cudaStream_t s);
-int clip_blocks_for(int precision, int slots, bool lean, int warps_per_block, int device);
+int clip_blocks_for(int precision, int slots, int form, int warps_per_block, int device);
 // CSR offsets (3 launches) and the gather into them (1 launch).
 cudaError_t launch_csr_offsets(const uint32_t* nface, uint32_t n, uint64_t* offs, uint64_t* scan_tmp,
                                cudaStream_t s);
