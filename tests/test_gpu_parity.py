@@ -205,6 +205,25 @@ def test_fp32_guard_reruns_on_lattice(tess, oracle_mod):
     assert same >= 0.95 * len(pts)
 
 
+def test_hybrid_rerun_on_bcc_lattice(tess, oracle_mod):
+    """Every cell of a 1e-7-jittered BCC lattice lands in the guard band: the
+    hybrid re-run decides those plane tests in FP64 and the cells keep their
+    FP32-form accuracy; the few it cannot settle run in FP64."""
+    from tessellator import workloads
+
+    pts = workloads.lattice_bcc(10, seed=6)
+    gpu, st = gpu_all(tess, pts, "fp32", container=unit_box(tess))
+    assert st["rerun_fp64"] == len(pts)
+    assert 0 <= st["rerun_fp64_full"] < st["rerun_fp64"]
+    assert st["failed"] == 0
+    vol, offs, nbr, area = gpu
+    rv, ro, ri, ra = ref_all(oracle_mod, pts, [0, 0, 0], [1, 1, 1])
+    assert np.max(np.abs(vol - rv) / rv) <= 1e-6
+    assert abs(vol.sum() - 1.0) < 1e-6
+    same = sum(np.array_equal(nbr[offs[i]:offs[i + 1]], ri[ro[i]:ro[i + 1]]) for i in range(len(pts)))
+    assert same >= 0.99 * len(pts)
+
+
 def test_clustered_small(tess, oracle_mod):
     from tessellator import workloads
 

@@ -157,6 +157,18 @@ __device__ __forceinline__ void emit_bins(const RadiusParams& p, bool keep, uint
     emit_stream<MODE, FILL>(p, beg, c, qt, pt_base, lane, w);
 }
 
+// A double to float, rounded toward zero, from the bit pattern alone (no
+// FP64-pipe conversion): |result| <= |v| and |v - result| < 2^-23 |v| in the
+// float range; below it 0 (error under 2^-126), above it (and NaN) +-inf.
+__device__ __forceinline__ float f64_to_f32_rz(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
+}
+
 __device__ __forceinline__ bool is_nan_bits(unsigned long long b) {
     return (b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
 }
@@ -315,18 +327,19 @@ __global__ void __launch_bounds__(256) k_radius(RadiusParams p) {
             const int k0 = __shfl_sync(kFull, idx, 5), i1 = __shfl_sync(kFull, idx, 6);
             const int j1 = __shfl_sync(kFull, idx, 7), k1 = __shfl_sync(kFull, idx, 8);
             if (MODE == RQ_REAL_RADIUS && p.f32_filter) {
-                // error band of the FP32 squared distance: per axis the two
-                // FP32 roundings of the coordinates plus the subtraction's,
-                // at most e = 2^-24 (|q| + |p| + |dq|) <= 6e-8 (2 m + 2.1 r);
-                // squared and summed near r^2 that is 2 sqrt(3) 1.01 r e + 3 e^2,
-                // plus 4 roundings of the sum and the FP64 side, doubled
-                const float fa = __double2float_rn(ca);           // one conversion per lane
+                // error band of the FP32 squared distance: per axis the query's
+                // truncation to FP32 (2^-23 |q|), the point's rounding
+                // (2^-24 |p|) and the subtraction's (2^-24 |dq|), at most
+                // e = 6e-8 (3 m + 2.1 r); squared and summed near r^2 that is
+                // 2 sqrt(3) 1.01 r e + 3 e^2, plus 4 roundings of the sum and
+                // the FP64 side, doubled
+                const float fa = f64_to_f32_rz(ca);                // integer ops, one coordinate per lane
                 qt.fx = __shfl_sync(kFull, fa, 0);
                 qt.fy = __shfl_sync(kFull, fa, 1);
                 qt.fz = __shfl_sync(kFull, fa, 2);
                 const float qmag = fmaxf(fmaxf(fabsf(qt.fx), fabsf(qt.fy)), fabsf(qt.fz));
                 const float m = fmaxf(gmag, qmag) * 1.0001f;
-                const float e = 6.0e-8f * (2.0f * m + 2.1f * fr);
+                const float e = 6.0e-8f * (3.0f * m + 2.1f * fr);
                 const float band = 2.0f * (3.5f * fr * e + 3.0f * e * e) + 1.0e-6f * r2f;
                 qt.lo_thr = r2f - band;
                 qt.hi_thr = r2f + band;
