@@ -57,7 +57,8 @@ typedef enum {
 
 /* Flags for tess_config.flags */
 #define TESS_FLAG_TIMING 1u     /* record per-pass device times (tess_stats)          */
-#define TESS_FLAG_COUNTERS 2u   /* count the clipping work (tess_stats, small overhead) */
+#define TESS_FLAG_COUNTERS 2u   /* count the clipping work (tess_stats); the FP32 first pass then runs
+                                   in its counting form, with the window pre-test (about 2% slower) */
 
 typedef struct {
     /* FP32 form, guard band: a plane test of vertex v is undecided (the cell

@@ -171,3 +171,32 @@ def test_timing_flag(tess, oracle_mod, prec):
     assert offs.astype(np.int64).tolist() == roffs.tolist()
     assert nbr.astype(np.int64).tolist() == rids.tolist()
     np.testing.assert_allclose(vol, rvol, rtol=1e-6 if prec == "fp32" else 1e-12)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_work_counters_flag(tess, prec):
+    """TESS_FLAG_COUNTERS counts the clipping work (every pass, every form)
+    and leaves the results as they are without it."""
+    rng = np.random.default_rng(34)
+    pts = rng.random((20000, 3))
+    box = tess.Polyhedron(0, 0, 0, 1, 1, 1)
+    with tess.Diagram(pts, container=box) as d:
+        d.compute_all(prec)
+        plain = (d.volumes(), *d.neighbors_csr())
+        assert d.stats()["candidates_tested"] == 0
+    cfg = tess.default_config(flags=tess.FLAG_COUNTERS)
+    with tess.Diagram(pts, container=box, config=cfg) as d:
+        d.compute_all(prec)
+        counted = (d.volumes(), *d.neighbors_csr())
+        st = d.stats()
+    n = len(pts)
+    assert 5 * n < st["cuts"] < 40 * n
+    assert st["cuts"] < st["candidates_tested"] < 200 * n
+    assert st["new_vertices"] > 2 * st["cuts"]
+    # the counting form may send a different few cells to a re-run: FP32-form
+    # values agree to their tolerance, neighbour lists exactly
+    tol = 1e-6 if prec == "fp32" else 0.0
+    np.testing.assert_allclose(counted[0], plain[0], rtol=tol)
+    assert np.array_equal(counted[1], plain[1]) and np.array_equal(counted[2], plain[2])
+    np.testing.assert_allclose(counted[3], plain[3], rtol=0, atol=1e-5 if prec == "fp32" else 0.0)
+

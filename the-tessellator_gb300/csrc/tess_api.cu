@@ -477,7 +477,10 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         // hybrid form (guard-band tests decided in FP64); what that cannot
         // settle runs in the FP64 form.
         const bool two = s0 < 4, one = s0 < 8;
-        TRY(pass(1, s0, s0 <= 2 ? kFormLean : kFormStd, nullptr, nullptr, L[L_FP64], cnt + L_FP64,
+        // (with TESS_FLAG_COUNTERS the first pass runs in the standard form:
+        // the lean form keeps no counters)
+        const bool lean = s0 <= 2 && !(E.cfg.flags & TESS_FLAG_COUNTERS);
+        TRY(pass(1, s0, lean ? kFormLean : kFormStd, nullptr, nullptr, L[L_FP64], cnt + L_FP64,
                  one ? L[L_CAP1] : nullptr, cnt + L_CAP1));
         if (timing) CU(cudaEventRecord(ev[1], E.stream));
         if (one) {

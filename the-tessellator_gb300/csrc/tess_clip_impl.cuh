@@ -220,7 +220,8 @@ __device__ __forceinline__ void bisector(double rx, double ry, double rz, double
 __device__ __forceinline__ float round_up_f(float x) { return x; }
 __device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
 
-// Per-warp work counters (reported when ClipParams::work is set).
+// Per-warp work counters (reported when ClipParams::work_ctr is set).  The
+// lean first-pass form does not count: the registers cost it 2%.
 struct Work {
     unsigned tested = 0, cuts = 0, newv = 0, windows = 0, batches = 0;
 };
@@ -953,7 +954,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         S.cbeg2[lane] = begB;
         __syncwarp();
         for (unsigned w0 = 0; w0 < total; w0 += 32) {
-            ++W.windows;
+            if constexpr (FORM != kFormLean) ++W.windows;
             const unsigned c = w0 + lane;
             bool keep = false;
             T rx = 0, ry = 0, rz = 0, r2 = 0;
@@ -1038,11 +1039,13 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 bisector(cx, cy, cz, c2, nx, ny, nz, off, rn);
                 const int r = cut<T, K, GUARD, FORM == kFormHybrid>(S, C, nx, ny, nz, off, rn, cR, cidb, cj, lane, P,
                                                                        fsite);
-                ++W.tested;
+                if constexpr (FORM != kFormLean) ++W.tested;
                 if (r < 0) return -r;
                 if (r > 0) {
-                    ++W.cuts;
-                    W.newv += (unsigned)(r - 1);
+                    if constexpr (FORM != kFormLean) {
+                        ++W.cuts;
+                        W.newv += (unsigned)(r - 1);
+                    }
                     const T R2b = R2;
                     R2 = live_r2(C, lane);
                     cR = (T)P.guard_rel * sqrt_up(R2);
@@ -1145,7 +1148,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             load_entry(t + lane, ea);
             if (kBatch2) load_entry(t + 32 + lane, eb);
         }
-        ++W.batches;
+        if constexpr (FORM != kFormLean) ++W.batches;
         status = process(ba, ca, bb, cb);
         if (status != ST_OK) break;
         if (!kPrefetch && !last) {
@@ -1177,7 +1180,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     if (key > D.tab_kmax && key < thr && !(radius >= 0.0 && key > radius)) lb = bin_of(i, j, k);
                 }
                 if (!__any_sync(FULL, lb >= 0)) continue;
-                ++W.batches;
+                if constexpr (FORM != kFormLean) ++W.batches;
                 unsigned beg = 0, cnt = 0;
                 if (lb >= 0) {
                     beg = P.delims[lb];
