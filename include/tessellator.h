@@ -61,9 +61,12 @@ typedef enum {
                                    in its counting form, with the window pre-test (about 2% slower) */
 
 typedef struct {
-    /* FP32 form, guard band: a plane test of vertex v is undecided (the cell
-     * re-runs in FP64) when |signed distance| <= e_v + guard_rel * R, with
-     * e_v the vertex's tracked error bound and R the cell radius. */
+    /* FP32 form, guard band: a plane test of vertex v against the bisector of
+     * the site and a point at offset r is undecided (the cell re-runs in FP64)
+     * when |signed distance| <= e_v + guard_rel * (|v|_1 + |r|) plus a small
+     * term for the FP32 split of the positions, with e_v the vertex's tracked
+     * error bound (distances normalised by |r|).  The FP32 rounding of a test
+     * stays below 3e-7 (|v|_1 + |r|): keep guard_rel at or above that. */
     double guard_rel;
     /* FP32 form, final check: the FP64 correction of every vertex must stay
      * within 2 e_v + verify_rel * R, else the cell re-runs in FP64. */
@@ -113,6 +116,10 @@ typedef struct {
     /* FP32 form: of the rerun_fp64 cells, those the hybrid re-run (guard-band
      * tests decided in FP64) could not settle, re-run entirely in FP64 */
     uint64_t rerun_fp64_full;
+    /* FP32 form: cells whose own bin is crowded (>= 48 points), taken out of
+     * the first pass and computed by a pass that first cuts by the nearest
+     * point of each lane's stride of that bin */
+    uint64_t dense_cells;
 } tess_stats;
 
 void tess_config_default(tess_config* cfg);

@@ -164,7 +164,8 @@ def test_timing_flag(tess, oracle_mod, prec):
             offs, nbr, area = d.neighbors_csr()
             st = d.stats()
             assert st["ms_grid"] > 0 and st["ms_clip"] > 0 and st["ms_csr"] > 0
-            d.find_neighbors_in_radius_batch(pts[:100], 0.03, True)
+            qo, qi = d.find_neighbors_in_radius_batch(pts[:20000], 0.03, True)
+            assert len(qi) > 20000 and qo[-1] == len(qi)
             assert d.stats()["ms_query_count"] > 0 and d.stats()["ms_query_fill"] > 0
         vol = d.volumes()
     rvol, roffs, rids, _, _, _ = oracle_mod.Diagram(pts, lo=[0, 0, 0], hi=[1, 1, 1]).compute_all()

@@ -225,6 +225,7 @@ def test_hybrid_rerun_on_bcc_lattice(tess, oracle_mod):
 
 
 def test_clustered_small(tess, oracle_mod):
+    """Crowded bins: the FP32 first pass hands their cells to the seeded pass."""
     from tessellator import workloads
 
     pts = workloads.clustered(20000, seed=3)
@@ -232,3 +233,52 @@ def test_clustered_small(tess, oracle_mod):
         gpu, st = gpu_all(tess, pts, prec, container=unit_box(tess))
         ref = ref_all(oracle_mod, pts, [0, 0, 0], [1, 1, 1])
         compare(prec, gpu, ref, len(pts), check_sum=1.0)
+        if prec == "fp32":
+            assert st["dense_cells"] > 1000
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_far_from_the_origin(tess, oracle_mod, prec):
+    """Coordinates near 1e6 in a unit box: the FP32 positions are split
+    relative to the diagram's centre, so the FP32 form keeps its accuracy."""
+    rng = np.random.default_rng(15)
+    lo = np.array([1.0e6, -2.0e6, 3.0e5])
+    pts = lo + rng.random((4000, 3))
+    gpu, st = gpu_all(tess, pts, prec, container=tess.Polyhedron(*lo, *(lo + 1)))
+    ref = ref_all(oracle_mod, pts, lo, lo + 1)
+    compare(prec, gpu, ref, len(pts), check_sum=1.0)
+    if prec == "fp32":
+        assert st["rerun_fp64"] < 0.05 * len(pts)
+
+
+def test_near_duplicates_fp32(tess, oracle_mod):
+    """Pairs 1e-12 .. 1e-5 apart and exact duplicates: the FP32 form hands the
+    cells of pairs nearer than ~1e-6 to the FP64 form (bit-identical results
+    there).  Cells bordering a pair meet two bisectors ~d apart, an
+    ill-conditioned sliver: elsewhere the bars are relaxed to 1e-9 (FP64 vs
+    the oracle) and 99% identical neighbour lists."""
+    rng = np.random.default_rng(16)
+    pts = rng.random((2000, 3))
+    k = 0
+    for d in (0.0, 1e-12, 1e-9, 1e-7, 1e-5):
+        for _ in range(4):
+            u = rng.standard_normal(3)
+            pts[k + 1] = pts[k] + d * u / np.linalg.norm(u)
+            k += 2
+    g32, st = gpu_all(tess, pts, "fp32", container=unit_box(tess))
+    g64, _ = gpu_all(tess, pts, "fp64", container=unit_box(tess))
+    assert st["rerun_fp64"] >= 32 and st["failed"] == 0
+    v32, o32, n32, _ = g32
+    v64, o64, n64, _ = g64
+    o32, o64 = o32.astype(np.int64), o64.astype(np.int64)
+
+    def lists(o, nb, i):
+        return nb[o[i]:o[i + 1]].tolist()
+
+    for i in range(32):                 # pairs 0 .. 1e-7 apart: computed in FP64
+        assert v32[i] == v64[i] and lists(o32, n32, i) == lists(o64, n64, i)
+    np.testing.assert_allclose(v32, v64, rtol=1e-6)
+    assert sum(lists(o32, n32, i) == lists(o64, n64, i) for i in range(len(pts))) >= 0.99 * len(pts)
+    rv, ro, ri, _ = ref_all(oracle_mod, pts, [0, 0, 0], [1, 1, 1])
+    np.testing.assert_allclose(v64, rv, rtol=1e-9)
+    assert sum(lists(o64, n64, i) == ri[ro[i]:ro[i + 1]].tolist() for i in range(len(pts))) >= 0.99 * len(pts)

@@ -69,8 +69,8 @@ int64_t cells_per_dim(uint64_t n, double density) {
 // Work lists of the re-run passes: FP64 (cells the FP32 passes flagged),
 // CAP1/CAP2 (FP32 capacity), CAP64A/B (FP64 capacity), FP64B (cells the
 // hybrid FP32 pass could not settle).
-enum { L_FP64 = 0, L_CAP1 = 1, L_CAP2 = 2, L_CAP64A = 3, L_CAP64B = 4, L_FP64B = 5, L_COUNT = 6, L_FAIL = 6,
-       L_REASON = 8 };
+enum { L_FP64 = 0, L_CAP1 = 1, L_CAP2 = 2, L_CAP64A = 3, L_CAP64B = 4, L_FP64B = 5, L_DENSE = 6, L_COUNT = 7,
+       L_FAIL = 7, L_REASON = 8 };
 // Kernels launched by one binning pass (launch_grid_build).
 constexpr uint64_t kGridLaunches = 11;
 
@@ -219,7 +219,7 @@ struct Engine {
 };
 
 void fill_defaults(tess_config* c) {
-    c->guard_rel = 1e-6;
+    c->guard_rel = 4e-7;
     c->verify_rel = 1e-6;
     c->bin_density = 1.25;
     c->table_gaps = 8;
@@ -453,8 +453,11 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
     // One launch over a work list (null: every cell).  Failed cells append to
     // the FP64 list (guard, degenerate, verify) and the capacity list.
     auto pass = [&](int prec, int slots, int form, const uint32_t* work, const unsigned* wcount, uint32_t* l64,
-                    unsigned* c64, uint32_t* lcap, unsigned* ccap) -> tess_status {
+                    unsigned* c64, uint32_t* lcap, unsigned* ccap, uint32_t* ldense = nullptr,
+                    unsigned* cdense = nullptr) -> tess_status {
         ClipParams p = base;
+        p.list_dense = ldense;
+        p.list_dense_count = cdense;
         p.work = work;
         p.work_count = wcount;
         p.cursor = cur + cursor++;
@@ -472,7 +475,8 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
     uint32_t* const* L = E.d_list;
     if (timing) CU(cudaEventRecord(ev[0], E.stream));
     if (precision == TESS_PRECISION_FP32_GUARD) {
-        // FP32: the lean first pass (2 slots per lane) over every cell;
+        // FP32: the lean first pass (2 slots per lane) over every cell but
+        // those of crowded bins, which run seeded in the standard form;
         // capacity re-runs at 4 and 8 slots; the flagged cells re-run in the
         // hybrid form (guard-band tests decided in FP64); what that cannot
         // settle runs in the FP64 form.
@@ -481,7 +485,9 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         // the lean form keeps no counters)
         const bool lean = s0 <= 2 && !(E.cfg.flags & TESS_FLAG_COUNTERS);
         TRY(pass(1, s0, lean ? kFormLean : kFormStd, nullptr, nullptr, L[L_FP64], cnt + L_FP64,
-                 one ? L[L_CAP1] : nullptr, cnt + L_CAP1));
+                 one ? L[L_CAP1] : nullptr, cnt + L_CAP1, lean ? L[L_DENSE] : nullptr, cnt + L_DENSE));
+        if (lean)
+            TRY(pass(1, 2, kFormStd, L[L_DENSE], cnt + L_DENSE, L[L_FP64], cnt + L_FP64, L[L_CAP1], cnt + L_CAP1));
         if (timing) CU(cudaEventRecord(ev[1], E.stream));
         if (one) {
             const int s1 = two ? 4 : 8;
@@ -546,10 +552,12 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
         if (precision == TESS_PRECISION_FP32_GUARD) {
             E.stats.rerun_fp64 = counts[L_FP64];
             E.stats.rerun_fp64_full = counts[L_FP64B];
+            E.stats.dense_cells = counts[L_DENSE];
             E.stats.rerun_capacity = (uint64_t)counts[L_CAP1] + counts[L_CAP2] + counts[L_CAP64A] + counts[L_CAP64B];
         } else {
             E.stats.rerun_fp64 = 0;
             E.stats.rerun_fp64_full = 0;
+            E.stats.dense_cells = 0;
             E.stats.rerun_capacity = (uint64_t)counts[L_CAP64A] + counts[L_CAP64B];
         }
         if (E.ndiag == 1) {
@@ -1333,7 +1341,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
         CU(cudaEventRecord(e0, E.stream));
     }
     CU(cudaGraphLaunch(E.graph, E.stream));
-    E.launches += kGridLaunches + (prec == 1 ? 6 : 3);
+    E.launches += kGridLaunches + (prec == 1 ? 7 : 3);
     if (timing) CU(cudaEventRecord(e1, E.stream));
     unsigned long long used = 0;
     unsigned counts[16];
@@ -1363,6 +1371,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
     E.stats.faces = used;
     E.stats.rerun_fp64 = prec == 1 ? counts[L_FP64] : 0;
     E.stats.rerun_fp64_full = prec == 1 ? counts[L_FP64B] : 0;
+    E.stats.dense_cells = prec == 1 ? counts[L_DENSE] : 0;
     E.stats.rerun_capacity = (uint64_t)counts[L_CAP1] + counts[L_CAP2] + counts[L_CAP64A] + counts[L_CAP64B];
     E.stats.failed = counts[L_FAIL];
     E.stats.rerun_guard = counts[L_REASON + ST_GUARD];

@@ -35,10 +35,15 @@
 // (the security radius; the reference walks every point instead,
 // celery.rs:971-1018, with the same result).
 //
-// FP32 form: positions, planes and classification in FP32; any live vertex
-// with |sd| below guard_rel * R (R = cell radius) aborts the cell, which is
-// then re-run in FP64.  Areas and volumes are accumulated in FP64 in both
-// forms (weighted normals and volume / 6, polyhedron.rs:776-855).
+// FP32 form: positions, planes and classification in FP32; a plane test
+// whose |sd| lies within its rigorous rounding bound (see cut()) aborts the
+// cell, which is then re-run with those tests decided in FP64 (or wholly in
+// FP64).  Areas and volumes are accumulated in FP64 in both forms (weighted
+// normals and volume / 6, polyhedron.rs:776-855).
+//
+// Crowded bins: a cell whose own bin holds many points is first cut by the
+// nearest point of each lane's stride of that bin (32 seeds, nearest first),
+// which shrinks it to about its final size before the shell walk.
 #include <cfloat>
 #include <cmath>
 
@@ -62,6 +67,15 @@ constexpr bool kPrefetch = true;
 // first-pass form leaves it out: on uniform inputs windows are small and its
 // mere presence costs the hot loop registers.
 constexpr int kPretestMin = 2;
+// A site whose own bin holds at least this many points is seeded before the
+// shell walk: every lane takes the nearest point of its stride of that bin and
+// the 32 seeds are cut nearest first.  In crowded bins the walk's 32-point
+// windows otherwise meet the nearest points late, after many cuts by farther
+// ones (plane capacity, larger radius, more guard-band tests).
+constexpr unsigned kSeedMin = 48;
+// Hybrid form: a new FP32 vertex whose error bound exceeds kNumBad * guard_rel
+// * R (1e-3 R at the default guard_rel) sends the cell to the FP64 form.
+constexpr float kNumBad = 2500.0f;
 
 template <typename T, int K>
 struct Smem {
@@ -278,7 +292,7 @@ struct Regs {
 template <typename T, int K, bool GUARD, bool RESOLVE>
 __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, const Regs<T, K> sdv,
                                         const Regs<uint32_t, K> omv, T nx, T ny, T nz, T off, T rn, T cR,
-                                        int32_t id, uint32_t src, int f, int lane) {
+                                        T gr, int32_t id, uint32_t src, int f, int lane) {
     using S_t = Smem<T, K>;
     const T(&sd)[K] = sdv.v;
     const uint32_t(&om)[K] = omv.v;
@@ -401,12 +415,15 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
                 py = (ah * bfy + bh * fay + off * aby) * inv;
                 pz = (ah * bfz + bh * faz + off * abz) * inv;
                 // e = kVertexErr |x|_1 / dhat, dhat = |det| / (|n_a| |n_b| |n_f|)
-                pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) * (S.pn[a] * S.pn[b] * rn) * fabs(inv);
+                const T x1 = fabs(px) + fabs(py) + fabs(pz);
+                pe = (T)kVertexErr * x1 * (S.pn[a] * S.pn[b] * rn) * fabs(inv);
                 if (!(pe < (T)1e30)) pe = (T)1e30;
                 // hybrid form: a cell that keeps going after FP64-decided
                 // tests must not carry an ill-conditioned (or non-finite)
                 // FP32 vertex; it re-runs in FP64 instead
-                if (RESOLVE && !(pe <= (T)1000 * cR)) numbad = true;
+                if (RESOLVE && !(pe <= (T)kNumBad * cR)) numbad = true;
+                // plus the vertex's share of a plane test's FP32 rounding
+                pe += gr * x1;
             } else {
                 const T den = xsd - ysd;
                 const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / den;
@@ -505,9 +522,18 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
 //     vertex is Outside when n.v - off > 1e-12 (vector3.rs:170-193,
 //     polyhedron.rs:221).
 //   FP32 form: n = r and off = r.r / 2 (the same plane, scaled by rn = |r|).
-//     Every vertex carries a bound e_v on its position error.  A test with
-//     |n.v - off| <= rn * (e_v + cR), cR bounding the plane's own rounding,
-//     cannot be decided in FP32: the cell goes to the FP64 form (ST_GUARD).
+//     Every vertex carries a bound e_v on its position error, to which
+//     guard_rel * |v|_1 is added at its creation.  A test with
+//     |n.v - off| <= rn * (e_v + guard_rel * rn) + eC cannot be decided in
+//     FP32: the cell goes to the FP64 form (ST_GUARD); eC covers the hi/lo
+//     split of the positions (see run_cell).  The bound on the FP32 test,
+//     with u = 2^-24, r~ the FP32 offset (|r~ - r| <= 2u |r|) and v~ the
+//     FP32 vertex (|v~ - v| <= e_v):
+//       fma chain rounding       3u (rn |v~|_1 + off)
+//       plane normal, vertex     2u rn |v|  +  rn e_v
+//       offset r.r / 2           3u rn^2
+//     <= rn (e_v + 5u |v~|_1 + 4.5u rn), about rn (e_v + 3e-7 (|v~|_1 + rn));
+//     the default guard_rel 4e-7 leaves a third in hand.
 // Returns 1 when vertices were cut off, 0 when nothing was Outside, or
 // -status.
 // FP64 view of the site and its container, for deciding guard-band plane
@@ -566,12 +592,15 @@ __device__ __noinline__ int resolve_fp64(const Smem<T, K>& S, const ClipParams& 
 }
 
 template <typename T, int K, bool GUARD, bool RESOLVE = false>
-__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T rn, T cR, int32_t id,
+__device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T rn, T cR, T eC, int32_t id,
                    uint32_t src, int lane, const ClipParams& P, const Fp64Site& site) {
     using S_t = Smem<T, K>;
     T sd[K];
     uint32_t om[K];
     bool gh = false;
+    // the plane's share of the test's FP32 rounding (FP32 form)
+    const T gr = GUARD ? (T)P.guard_rel : (T)0;
+    const T rc = gr * rn;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         sd[k] = (T)0;
@@ -583,7 +612,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         const bool live = (C.lm[k] >> lane) & 1u;
         sd[k] = sdist(nx, ny, nz, off, C.vx[k], C.vy[k], C.vz[k]);
         const bool out = live && sd[k] > (GUARD ? (T)0 : (T)kTolerance);
-        if constexpr (GUARD) gh |= live && fabs(sd[k]) <= rn * (C.ve[k] + cR);
+        if constexpr (GUARD) gh |= live && fabs(sd[k]) <= fma(rn, C.ve[k] + rc, eC);
         om[k] = __ballot_sync(FULL, out);
     }
     if (GUARD && __any_sync(FULL, gh)) {
@@ -597,7 +626,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             for (int k = 0; k < K; ++k) {
                 if (C.lm[k] == 0) continue;
                 const bool live = (C.lm[k] >> lane) & 1u;
-                const bool amb = live && fabs(sd[k]) <= rn * (C.ve[k] + cR);
+                const bool amb = live && fabs(sd[k]) <= fma(rn, C.ve[k] + rc, eC);
                 bool out = live && sd[k] > (T)0;
                 if (amb) {
                     const int r = resolve_fp64<T, K>(S, P, site, k * 32 + lane, src);
@@ -690,12 +719,15 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
                 py = (ah * bfy + bh * fay + off * aby) * inv;
                 pz = (ah * bfz + bh * faz + off * abz) * inv;
                 // e = kVertexErr |x|_1 / dhat, dhat = |det| / (|n_a| |n_b| |n_f|)
-                pe = (T)kVertexErr * (fabs(px) + fabs(py) + fabs(pz)) * (S.pn[a] * S.pn[b] * rn) * fabs(inv);
+                const T x1 = fabs(px) + fabs(py) + fabs(pz);
+                pe = (T)kVertexErr * x1 * (S.pn[a] * S.pn[b] * rn) * fabs(inv);
                 if (!(pe < (T)1e30)) pe = (T)1e30;
                 // hybrid form: a cell that keeps going after FP64-decided
                 // tests must not carry an ill-conditioned (or non-finite)
                 // FP32 vertex; it re-runs in FP64 instead
-                if (RESOLVE && !(pe <= (T)1000 * cR)) numbad = true;
+                if (RESOLVE && !(pe <= (T)kNumBad * cR)) numbad = true;
+                // plus the vertex's share of a plane test's FP32 rounding
+                pe += gr * x1;
             } else {
                 const T xx = S.vx[x], xy = S.vy[x], xz = S.vz[x], xsd = S.vsd[x];
                 const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
@@ -770,7 +802,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         sdv.v[k] = sd[k];
         omv.v[k] = om[k];
     }
-    return cut_general<T, K, GUARD, RESOLVE>(S, C, sdv, omv, nx, ny, nz, off, rn, cR, id, src, f, lane);
+    return cut_general<T, K, GUARD, RESOLVE>(S, C, sdv, omv, nx, ny, nz, off, rn, cR, gr, id, src, f, lane);
 }
 
 // Squared radius of the cell about its site: max |v|^2 over live vertices;
@@ -826,6 +858,9 @@ template <typename T, int K, bool GEO, int FORM>
 __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int lane, Work& W) {
     using S_t = Smem<T, K>;
     constexpr bool GUARD = sizeof(T) == 4;
+    // the lean first pass sends crowded cells to a seeded pass instead (the
+    // seeding code would cost its hot loop registers)
+    constexpr bool kSeedForm = FORM != kFormLean;
     // ---- diagram of this cell ----
     int d = 0;
     if (P.ndiag > 1 && !P.at_point) {
@@ -854,14 +889,16 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         self = gs;
         orig = P.sorted[gs];
     }
-    // FP32 form: the site as an FP32 pair (hi + lo), so candidate offsets
-    // (p - site) come out of FP32 arithmetic with FP64-rounded accuracy.
+    // FP32 form: the site as an FP32 pair (hi + lo) relative to the diagram's
+    // centre, like the points, so candidate offsets (p - site) come out of
+    // FP32 arithmetic nearly as accurate as FP64's.
     float shx = 0.f, shy = 0.f, shz = 0.f, slx = 0.f, sly = 0.f, slz = 0.f;
     if constexpr (GUARD) {
         if (P.at_point) {
-            shx = __double2float_rn(sx); slx = __double2float_rn(sx - (double)shx);
-            shy = __double2float_rn(sy); sly = __double2float_rn(sy - (double)shy);
-            shz = __double2float_rn(sz); slz = __double2float_rn(sz - (double)shz);
+            const double ux = sx - D.ctr[0], uy = sy - D.ctr[1], uz = sz - D.ctr[2];
+            shx = __double2float_rn(ux); slx = __double2float_rn(ux - (double)shx);
+            shy = __double2float_rn(uy); sly = __double2float_rn(uy - (double)shy);
+            shz = __double2float_rn(uz); slz = __double2float_rn(uz - (double)shz);
         } else {
             shx = P.shi[3ull * gs]; shy = P.shi[3ull * gs + 1]; shz = P.shi[3ull * gs + 2];
             slx = P.slo[3ull * gs]; sly = P.slo[3ull * gs + 1]; slz = P.slo[3ull * gs + 2];
@@ -904,7 +941,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         S.vz[lane] = C.vz[0];
         if constexpr (GUARD) {
             // rounding of the FP64 box corner to FP32
-            C.ve[0] = (T)1.2e-7 * (fabs(C.vx[0]) + fabs(C.vy[0]) + fabs(C.vz[0]));
+            C.ve[0] = ((T)1.2e-7 + (T)P.guard_rel) * (fabs(C.vx[0]) + fabs(C.vy[0]) + fabs(C.vz[0]));
             S.ve[lane] = C.ve[0];
         }
         const int pX = bx, pY = 2 + by, pZ = 4 + bz;
@@ -925,8 +962,25 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     for (int i = lane; i < C.nfree; i += 32) S.fl[i] = (uint8_t)(S_t::VUSE - 1 - i);
     __syncwarp();
     T R2 = live_r2(C, lane);
-    // cR: bound on the FP32 rounding of one plane test, relative to the cell radius
+    // guard_rel * cell radius: the hybrid form's limit on a vertex's error bound
     T cR = (T)P.guard_rel * sqrt_up(R2);
+    // FP32 form, the hi/lo split's share of a plane test's error (u = 2^-24,
+    // positions relative to the diagram's centre): per component the offset
+    // r~ = (hi_p - hi_s) + (lo_p - lo_s) is off by at most 2u |r| (relative,
+    // in the bound of a test) plus eta = 6.1 u^2 (|site|_inf + R) (the lo
+    // parts' rounding, the hi subtraction's share of it, the FP64 centring),
+    // which moves n.v - off by at most eta (|v|_1 + 1.8 rn) <= 5.4 eta R.
+    // R only shrinks, so the initial radius bounds it for the whole cell.
+    // Candidates nearer than 4 eta / u (plane error above u/4 relative, beyond
+    // the vertex error model) send the cell to the FP64 form.
+    T eC = 0, dup2 = 0;
+    if constexpr (GUARD) {
+        const float sa = fmaxf(fabsf(shx), fmaxf(fabsf(shy), fabsf(shz))) * 1.001f;
+        const T R = sqrt_up(R2) * (T)1.001;
+        eC = (T)1.3e-13 * (sa + R) * R;
+        const T d = (T)1.5e-6 * (sa + R);
+        dup2 = d * d;
+    }
     int status = ST_OK;
 
     // ---- the walk over bins in shell order (celery.rs:1023-1075) ----
@@ -938,6 +992,98 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     const bool has_radius = radius >= 0.0;
     const int64_t tgroup = P.target_group;
     const TabEntry* tab = P.table + D.tab_base;
+
+    // The offset p - site of sorted point j and its squared length.
+    auto cand = [&](uint32_t j, T& rx, T& ry, T& rz, T& r2) {
+        if constexpr (GUARD) {
+            rx = (T)((P.shi[3ull * j] - shx) + (P.slo[3ull * j] - slx));
+            ry = (T)((P.shi[3ull * j + 1] - shy) + (P.slo[3ull * j + 1] - sly));
+            rz = (T)((P.shi[3ull * j + 2] - shz) + (P.slo[3ull * j + 2] - slz));
+        } else {
+            rx = (T)(P.spx[j] - sx);
+            ry = (T)(P.spy[j] - sy);
+            rz = (T)(P.spz[j] - sz);
+        }
+        r2 = rx * rx + ry * ry + rz * rz;
+    };
+    // Sorted index of the lane's seed (none: ~0u); never a window candidate.
+    uint32_t seedj = 0xFFFFFFFFu;
+
+    // One window: up to one candidate per lane (keep), cut nearest first.
+    auto run_window = [&](bool keep, T rx, T ry, T rz, T r2, uint32_t j, int32_t cid) -> int {
+        unsigned km = __ballot_sync(FULL, keep);
+        // Pre-test the window at once: each lane tests its own candidate's
+        // bisector against every live vertex (read from the shared
+        // mirror).  A bisector with no vertex Outside cuts nothing now and
+        // nothing later (the cell only shrinks), so only possible cutters
+        // (and guard-band cases, which the serial test reports) go on to
+        // the serial nearest-first loop.  Same arithmetic as cut().
+        if (FORM != kFormLean && __popc(km) >= kPretestMin) {
+            bool maycut = false;
+            if (keep) {
+                T nx_, ny_, nz_, off_, rn_;
+                bisector(rx, ry, rz, r2, nx_, ny_, nz_, off_, rn_);
+                bool out = false, amb = false;
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    uint32_t m = C.lm[k];
+                    while (m) {
+                        const int sl = k * 32 + __ffs(m) - 1;
+                        m &= m - 1u;
+                        const T sd = sdist(nx_, ny_, nz_, off_, S.vx[sl], S.vy[sl], S.vz[sl]);
+                        out |= sd > (GUARD ? (T)0 : (T)kTolerance);
+                        if constexpr (GUARD) amb |= fabs(sd) <= fma(rn_, S.ve[sl] + (T)P.guard_rel * rn_, eC);
+                    }
+                }
+                maycut = out || amb;
+            }
+            km = __ballot_sync(FULL, keep && maycut);
+        }
+        // Nearest first: repeatedly take the closest remaining candidate
+        // (warp minimum of its distance, ties by lane), so the closest
+        // bisectors shrink the cell before the farther ones are tested.
+        // The key keeps the top 27 bits of r2 (a positive float orders
+        // like its bits) and the lane in the low 5.
+        const unsigned mykey = (__float_as_uint((float)r2) & ~31u) | (unsigned)lane;
+        while (km) {
+            const unsigned best = __reduce_min_sync(FULL, ((km >> lane) & 1u) ? mykey : 0xFFFFFFFFu);
+            const int src = (int)(best & 31u);
+            km &= ~(1u << src);
+            const T cx = __shfl_sync(FULL, rx, src);
+            const T cy = __shfl_sync(FULL, ry, src);
+            const T cz = __shfl_sync(FULL, rz, src);
+            const T c2 = __shfl_sync(FULL, r2, src);
+            const uint32_t cj = __shfl_sync(FULL, j, src);
+            const int32_t cidb = __shfl_sync(FULL, cid, src);
+            const T lim2 = (T)4 * R2 * (T)kStopMargin;
+            if (!(c2 < lim2)) {
+                // taken in increasing distance: the rest are farther still
+                if (c2 > lim2 * (T)1.001) km = 0;
+                continue;
+            }
+            T nx, ny, nz, off, rn;
+            bisector(cx, cy, cz, c2, nx, ny, nz, off, rn);
+            const int r = cut<T, K, GUARD, FORM == kFormHybrid>(S, C, nx, ny, nz, off, rn, cR, eC, cidb, cj, lane,
+                                                                   P, fsite);
+            if constexpr (FORM != kFormLean) ++W.tested;
+            if (r < 0) return -r;
+            if (r > 0) {
+                if constexpr (FORM != kFormLean) {
+                    ++W.cuts;
+                    W.newv += (unsigned)(r - 1);
+                }
+                const T R2b = R2;
+                R2 = live_r2(C, lane);
+                cR = (T)P.guard_rel * sqrt_up(R2);
+                // hybrid form: a cut never moves a vertex beyond the cell
+                // (convexity), so a radius that grew (or is no longer
+                // finite) means an FP32 vertex went wrong after an
+                // FP64-decided test; the cell re-runs in FP64
+                if (FORM == kFormHybrid && !(R2 <= R2b * (T)1.001)) return ST_GUARD;
+            }
+        }
+        return ST_OK;
+    };
 
     // Cut by every point of the lane's two bins, given as sorted ranges
     // [begA, begA + cntA) and [begB, begB + cntB).
@@ -961,6 +1107,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             uint32_t j = 0;
             int32_t cid = 0;
             const T lim = (T)4 * R2 * (T)kStopMargin;
+            bool near = false;
             if (c < total) {
                 const bool second = c >= totala;
                 const uint32_t* pref = second ? S.ccnt : S.cpref;
@@ -971,91 +1118,16 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     else hi = mid - 1;
                 }
                 j = (second ? S.cbeg2[lo] : S.cbeg[lo]) + (c - pref[lo]);
-                if constexpr (GUARD) {
-                    rx = (T)((P.shi[3ull * j] - shx) + (P.slo[3ull * j] - slx));
-                    ry = (T)((P.shi[3ull * j + 1] - shy) + (P.slo[3ull * j + 1] - sly));
-                    rz = (T)((P.shi[3ull * j + 2] - shz) + (P.slo[3ull * j + 2] - slz));
-                } else {
-                    rx = (T)(P.spx[j] - sx);
-                    ry = (T)(P.spy[j] - sy);
-                    rz = (T)(P.spz[j] - sz);
-                }
-                r2 = rx * rx + ry * ry + rz * rz;
-                keep = (j != self) && r2 > (T)0 && r2 < lim;
+                cand(j, rx, ry, rz, r2);
+                keep = (j != self) && r2 > dup2 && r2 < lim;
+                if constexpr (GUARD) near = (j != self) && !(r2 > dup2);
+                if constexpr (kSeedForm) keep = keep && j != seedj;
                 cid = (int32_t)(P.sorted[j] - pt_base);
                 if (keep && tgroup >= 0) keep = (int64_t)(P.sgroup ? P.sgroup[j] : 0u) == tgroup;
             }
-            unsigned km = __ballot_sync(FULL, keep);
-            // Pre-test the window at once: each lane tests its own candidate's
-            // bisector against every live vertex (read from the shared
-            // mirror).  A bisector with no vertex Outside cuts nothing now and
-            // nothing later (the cell only shrinks), so only possible cutters
-            // (and guard-band cases, which the serial test reports) go on to
-            // the serial nearest-first loop.  Same arithmetic as cut().
-            if (FORM != kFormLean && __popc(km) >= kPretestMin) {
-                bool maycut = false;
-                if (keep) {
-                    T nx_, ny_, nz_, off_, rn_;
-                    bisector(rx, ry, rz, r2, nx_, ny_, nz_, off_, rn_);
-                    bool out = false, amb = false;
-#pragma unroll
-                    for (int k = 0; k < K; ++k) {
-                        uint32_t m = C.lm[k];
-                        while (m) {
-                            const int sl = k * 32 + __ffs(m) - 1;
-                            m &= m - 1u;
-                            const T sd = sdist(nx_, ny_, nz_, off_, S.vx[sl], S.vy[sl], S.vz[sl]);
-                            out |= sd > (GUARD ? (T)0 : (T)kTolerance);
-                            if constexpr (GUARD) amb |= fabs(sd) <= rn_ * (S.ve[sl] + cR);
-                        }
-                    }
-                    maycut = out || amb;
-                }
-                km = __ballot_sync(FULL, keep && maycut);
-            }
-            // Nearest first: repeatedly take the closest remaining candidate
-            // (warp minimum of its distance, ties by lane), so the closest
-            // bisectors shrink the cell before the farther ones are tested.
-            // The key keeps the top 27 bits of r2 (a positive float orders
-            // like its bits) and the lane in the low 5.
-            const unsigned mykey = (__float_as_uint((float)r2) & ~31u) | (unsigned)lane;
-            while (km) {
-                const unsigned best = __reduce_min_sync(FULL, ((km >> lane) & 1u) ? mykey : 0xFFFFFFFFu);
-                const int src = (int)(best & 31u);
-                km &= ~(1u << src);
-                const T cx = __shfl_sync(FULL, rx, src);
-                const T cy = __shfl_sync(FULL, ry, src);
-                const T cz = __shfl_sync(FULL, rz, src);
-                const T c2 = __shfl_sync(FULL, r2, src);
-                const uint32_t cj = __shfl_sync(FULL, j, src);
-                const int32_t cidb = __shfl_sync(FULL, cid, src);
-                const T lim2 = (T)4 * R2 * (T)kStopMargin;
-                if (!(c2 < lim2)) {
-                    // taken in increasing distance: the rest are farther still
-                    if (c2 > lim2 * (T)1.001) km = 0;
-                    continue;
-                }
-                T nx, ny, nz, off, rn;
-                bisector(cx, cy, cz, c2, nx, ny, nz, off, rn);
-                const int r = cut<T, K, GUARD, FORM == kFormHybrid>(S, C, nx, ny, nz, off, rn, cR, cidb, cj, lane, P,
-                                                                       fsite);
-                if constexpr (FORM != kFormLean) ++W.tested;
-                if (r < 0) return -r;
-                if (r > 0) {
-                    if constexpr (FORM != kFormLean) {
-                        ++W.cuts;
-                        W.newv += (unsigned)(r - 1);
-                    }
-                    const T R2b = R2;
-                    R2 = live_r2(C, lane);
-                    cR = (T)P.guard_rel * sqrt_up(R2);
-                    // hybrid form: a cut never moves a vertex beyond the cell
-                    // (convexity), so a radius that grew (or is no longer
-                    // finite) means an FP32 vertex went wrong after an
-                    // FP64-decided test; the cell re-runs in FP64
-                    if (FORM == kFormHybrid && !(R2 <= R2b * (T)1.001)) return ST_GUARD;
-                }
-            }
+            if (GUARD && __any_sync(FULL, near)) return ST_GUARD;
+            const int st = run_window(keep, rx, ry, rz, r2, j, cid);
+            if (st != ST_OK) return st;
         }
         __syncwarp();
         return ST_OK;
@@ -1121,13 +1193,43 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             }
         }
     };
+    // ---- seeds from a crowded own bin ----
+    if constexpr (FORM != kFormLean) {
+        {   // the site's bin (axis_index clamps to the grid; its gap key -1 is always walked)
+            const uint64_t sb = bin_base + ((uint64_t)cbx * cpd + cby) * cpd + cbz;
+            const unsigned sbeg = P.delims[sb], scnt = P.delims[sb + 1] - sbeg;
+            if (scnt >= kSeedMin) {
+                T brx = 0, bry = 0, brz = 0, br2 = (T)INFINITY;
+                for (unsigned q = lane; q < scnt; q += 32) {
+                    const uint32_t j = sbeg + q;
+                    T rx, ry, rz, r2;
+                    cand(j, rx, ry, rz, r2);
+                    bool keep = (j != self) && r2 > dup2 && r2 < br2;
+                    if (keep && tgroup >= 0) keep = (int64_t)(P.sgroup ? P.sgroup[j] : 0u) == tgroup;
+                    if (keep) {
+                        brx = rx;
+                        bry = ry;
+                        brz = rz;
+                        br2 = r2;
+                        seedj = j;
+                    }
+                }
+                const bool has = seedj != 0xFFFFFFFFu;
+                const int32_t bcid = has ? (int32_t)(P.sorted[seedj] - pt_base) : 0;
+                status = run_window(has, brx, bry, brz, br2, seedj, bcid);
+            }
+        }
+    }
     Ent ea, eb;
     eb.i = eb.j = eb.k = 0;
     eb.key = INFINITY;
     eb.beg = eb.cnt = 0;
     load_entry(lane, ea);
     if (kBatch2) load_entry(32 + lane, eb);
-    for (;;) {
+    // lean first pass: a crowded own bin (table entry 0, lane 0's first
+    // entry) sends the cell to the seeded pass
+    if (FORM == kFormLean && P.list_dense && __shfl_sync(FULL, ea.cnt, 0) >= kSeedMin) status = ST_DENSE;
+    while (status == ST_OK) {
         // The table key is rounded toward zero and the threshold up, so
         // stopping on key >= thr never drops a bin that could hold a cutter.
         const float thr = round_up_f((T)4 * R2 * (T)kStopMargin);
@@ -1394,6 +1496,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             } else if (status == ST_VCAP || status == ST_PCAP) {
                 list = P.list_cap;
                 count = P.list_cap_count;
+            } else if (status == ST_DENSE) {
+                list = P.list_dense;
+                count = P.list_dense_count;
             }
             if (list) {
                 list[atomicAdd(count, 1u)] = gs;

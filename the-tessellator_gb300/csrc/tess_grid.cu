@@ -74,6 +74,8 @@ __global__ void k_grid_params(GridBuffers g) {
         const double hi = ord_dec(g.bounds[6 * d + 3 + a]);
         D.glo[a] = lo;
         D.ghi[a] = hi;
+        const double ctr = 0.5 * lo + 0.5 * hi;
+        D.ctr[a] = isfinite(ctr) ? ctr : 0.0;
         const double ext = __dsub_rn(hi, lo);
         D.size[a] = __ddiv_rn(ext, c);
         D.inv[a] = __ddiv_rn(c, ext);
@@ -217,6 +219,9 @@ __global__ void k_bin_order(GridBuffers g) {
 }
 
 // Positions (and groups) in sorted order, SoA for coalesced candidate loads.
+// The FP32 pair (hi, lo) splits the position relative to its diagram's
+// centre: the split keeps 48 bits of that offset, so its error scales with
+// the diagram's extent rather than with the coordinates' distance from 0.
 __global__ void k_gather(GridBuffers g) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.total) return;
@@ -226,13 +231,21 @@ __global__ void k_gather(GridBuffers g) {
     g.spx[s] = x;
     g.spy[s] = y;
     g.spz[s] = z;
-    const float hx = __double2float_rn(x), hy = __double2float_rn(y), hz = __double2float_rn(z);
+    int lo = 0, hi = g.ndiag - 1;     // the diagram holding sorted position s
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (g.diags[mid].pt_base <= s) lo = mid;
+        else hi = mid - 1;
+    }
+    const DiagDesc& D = g.diags[lo];
+    const double ux = x - D.ctr[0], uy = y - D.ctr[1], uz = z - D.ctr[2];
+    const float hx = __double2float_rn(ux), hy = __double2float_rn(uy), hz = __double2float_rn(uz);
     g.shi[3ull * s] = hx;
     g.shi[3ull * s + 1] = hy;
     g.shi[3ull * s + 2] = hz;
-    g.slo[3ull * s] = __double2float_rn(x - (double)hx);
-    g.slo[3ull * s + 1] = __double2float_rn(y - (double)hy);
-    g.slo[3ull * s + 2] = __double2float_rn(z - (double)hz);
+    g.slo[3ull * s] = __double2float_rn(ux - (double)hx);
+    g.slo[3ull * s + 1] = __double2float_rn(uy - (double)hy);
+    g.slo[3ull * s + 2] = __double2float_rn(uz - (double)hz);
     if (g.sgroup) g.sgroup[s] = g.groups[i];
 }
 

@@ -33,6 +33,7 @@ enum CellStatus : uint8_t {
     ST_DEGEN = 4,       // inconsistent topology (degenerate input) -> FP64 re-run / error
     ST_POOL = 5,        // face pool full -> host grows the pool
     ST_VERIFY = 6,      // FP32 vertex failed the FP64 check -> FP64 re-run
+    ST_DENSE = 7,       // crowded own bin (lean first pass) -> seeded re-run
     ST_PENDING = 255    // not computed yet
 };
 
@@ -40,6 +41,7 @@ enum CellStatus : uint8_t {
 // bases, box) and partly on the device (bounds, bin sizes, table length).
 struct DiagDesc {
     double glo[3], ghi[3];   // CeleryBounds (celery.rs:81-125), tight point bounds
+    double ctr[3];           // centre of those bounds: the FP32 hi/lo positions are split relative to it
     double size[3];          // x/y/z_cell_size (celery.rs:165-167)
     double inv[3];           // x/y/z_inverse_cell_size (celery.rs:169-171)
     double blo[3], bhi[3];   // container box (walls)
@@ -246,6 +248,8 @@ struct ClipParams {
     unsigned int* list_fp64_count;
     uint32_t* list_cap;           // capacity overflow cells or null
     unsigned int* list_cap_count;
+    uint32_t* list_dense;         // lean first pass: cells of crowded bins, or null
+    unsigned int* list_dense_count;
     unsigned int* fail_count;     // cells left with an error status
     unsigned int* reasons;        // per status code: cells routed or failed for it
     unsigned long long* work_ctr; // optional work counters (tested, cuts, new vertices, windows, batches)

@@ -239,13 +239,16 @@ __global__ void __launch_bounds__(256) k_radius(RadiusParams p) {
     const unsigned long long clamp_bits =
         (unsigned long long)__double_as_longlong(kind == 2 ? D.ghi[ax] : D.glo[ax]);
     const unsigned long long clamp_code = (clamp_bits >> 63) ? ~clamp_bits : (clamp_bits | 0x8000000000000000ull);
-    const double delta = kind == 1 ? -r : (kind == 2 ? r : 0.0);
+    // lanes 9-11 form the query relative to the diagram's centre (the frame
+    // of the points' FP32 parts) in the same FP64 add
+    const double delta = kind == 1 ? -r : (kind == 2 ? r : (lane >= 9 && lane < 12 ? -D.ctr[ax] : 0.0));
     int top = 1;
     while (2 * top < cpd) top *= 2;
-    // magnitude bound of the point coordinates, and the radius, for the FP32
-    // filter's error band
-    const float gmag = (float)fmax(fmax(fmax(fabs(D.glo[0]), fabs(D.ghi[0])), fmax(fabs(D.glo[1]), fabs(D.ghi[1]))),
-                                   fmax(fabs(D.glo[2]), fabs(D.ghi[2])));
+    // magnitude bound of the point coordinates relative to the centre, and
+    // the radius, for the FP32 filter's error band
+    double gm = 0.0;
+    for (int a = 0; a < 3; ++a) gm = fmax(gm, fmax(fabs(D.glo[a] - D.ctr[a]), fabs(D.ghi[a] - D.ctr[a])));
+    const float gmag = (float)gm;
     const float fr = (float)r;
     const float r2f = (float)r2;
 
@@ -327,16 +330,18 @@ __global__ void __launch_bounds__(256) k_radius(RadiusParams p) {
             const int k0 = __shfl_sync(kFull, idx, 5), i1 = __shfl_sync(kFull, idx, 6);
             const int j1 = __shfl_sync(kFull, idx, 7), k1 = __shfl_sync(kFull, idx, 8);
             if (MODE == RQ_REAL_RADIUS && p.f32_filter) {
-                // error band of the FP32 squared distance: per axis the query's
-                // truncation to FP32 (2^-23 |q|), the point's rounding
-                // (2^-24 |p|) and the subtraction's (2^-24 |dq|), at most
+                // error band of the FP32 squared distance, q and p relative to
+                // the diagram's centre (each FP64-rounded, 2^-53 |q|): per axis
+                // the query's truncation to FP32 (2^-23 |q|), the point's
+                // rounding (2^-24 |p|) and the subtraction's (2^-24 |dq|), at most
                 // e = 6e-8 (3 m + 2.1 r); squared and summed near r^2 that is
                 // 2 sqrt(3) 1.01 r e + 3 e^2, plus 4 roundings of the sum and
                 // the FP64 side, doubled
-                const float fa = f64_to_f32_rz(ca);                // integer ops, one coordinate per lane
-                qt.fx = __shfl_sync(kFull, fa, 0);
-                qt.fy = __shfl_sync(kFull, fa, 1);
-                qt.fz = __shfl_sync(kFull, fa, 2);
+                // integer ops, the centre-relative coordinates of lanes 9-11
+                const float fa = f64_to_f32_rz(__longlong_as_double((long long)vb));
+                qt.fx = __shfl_sync(kFull, fa, 9);
+                qt.fy = __shfl_sync(kFull, fa, 10);
+                qt.fz = __shfl_sync(kFull, fa, 11);
                 const float qmag = fmaxf(fmaxf(fabsf(qt.fx), fabsf(qt.fy)), fabsf(qt.fz));
                 const float m = fmaxf(gmag, qmag) * 1.0001f;
                 const float e = 6.0e-8f * (3.0f * m + 2.1f * fr);

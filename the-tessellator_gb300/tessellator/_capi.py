@@ -51,7 +51,8 @@ class Stats(C.Structure):
                 ("rerun_guard", C.c_uint64), ("rerun_verify", C.c_uint64), ("rerun_degenerate", C.c_uint64),
                 ("candidates_tested", C.c_uint64), ("cuts", C.c_uint64), ("new_vertices", C.c_uint64),
                 ("windows", C.c_uint64), ("batches", C.c_uint64), ("ms_query_count", C.c_double),
-                ("ms_query_fill", C.c_double), ("rerun_fp64_full", C.c_uint64)]
+                ("ms_query_fill", C.c_double), ("rerun_fp64_full", C.c_uint64),
+                ("dense_cells", C.c_uint64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
