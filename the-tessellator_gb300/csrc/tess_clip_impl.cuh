@@ -1175,6 +1175,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         float key;
         unsigned beg, cnt;
     };
+    uint32_t done = 0;   // crowded bins already handled (see below)
     auto load_entry = [&](uint32_t idx, Ent& e) {
         e.i = e.j = e.k = 0;
         e.key = INFINITY;
@@ -1186,20 +1187,48 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             e.k = te.k;
             e.key = te.key;
             if (has_radius && gap_key(D.size, e.i, e.j, e.k) > radius) e.key = INFINITY;
-            const long long lb = bin_of(e.i, e.j, e.k);
+            long long lb = bin_of(e.i, e.j, e.k);
+            if (kSeedForm && done && abs(e.i) <= 1 && abs(e.j) <= 1 && abs(e.k) <= 1 &&
+                ((done >> ((e.i + 1) * 9 + (e.j + 1) * 3 + (e.k + 1))) & 1u))
+                lb = -1;   // handled among the crowded bins
             if (lb >= 0) {
                 e.beg = P.delims[lb];
                 e.cnt = P.delims[lb + 1] - e.beg;
             }
         }
     };
-    // ---- seeds from a crowded own bin ----
-    if constexpr (FORM != kFormLean) {
-        {   // the site's bin (axis_index clamps to the grid; its gap key -1 is always walked)
-            const uint64_t sb = bin_base + ((uint64_t)cbx * cpd + cby) * cpd + cbz;
-            const unsigned sbeg = P.delims[sb], scnt = P.delims[sb + 1] - sbeg;
-            if (scnt >= kSeedMin) {
+    // ---- crowded bins first ----
+    // When the site's own bin is crowded, it and every crowded neighbour bin
+    // still within reach are handled here one at a time, nearest first: the
+    // 32 seeds (the nearest point of each lane's stride of the bin) are cut
+    // nearest first, then the bin's windows, each lane skipping its own seed
+    // (window lane = position mod 32, the seed's stride).  The shell walk
+    // skips the bins done here (27-bit mask `done` over the offsets {-1,0,1}^3).
+    if constexpr (kSeedForm) {
+        const uint64_t sb = bin_base + ((uint64_t)cbx * cpd + cby) * cpd + cbz;
+        if (P.delims[sb + 1] - P.delims[sb] >= kSeedMin) {
+            const int ti = lane / 9 - 1, tj = (lane / 3) % 3 - 1, tk = lane % 3 - 1;
+            unsigned nbeg = 0, ncnt = 0;
+            float nd = INFINITY;
+            if (lane < 27) {
+                const long long lb = bin_of(ti, tj, tk);
+                if (lb >= 0 && !(has_radius && gap_key(D.size, ti, tj, tk) > radius)) {
+                    nbeg = P.delims[lb];
+                    ncnt = P.delims[lb + 1] - nbeg;
+                }
+                nd = lane == 13 ? 0.f : (near_ok ? near2(ti, tj, tk) : INFINITY);
+            }
+            unsigned pending = __ballot_sync(FULL, ncnt >= kSeedMin && nd < INFINITY);
+            const unsigned ndkey = (__float_as_uint(nd) & ~31u) | (unsigned)lane;
+            while (pending && status == ST_OK) {
+                const unsigned best = __reduce_min_sync(FULL, ((pending >> lane) & 1u) ? ndkey : 0xFFFFFFFFu);
+                const int t = (int)(best & 31u);
+                pending &= ~(1u << t);
+                // still within reach of the (shrinking) cell?
+                if (t != 13 && __shfl_sync(FULL, nd, t) * (1.0f - 1e-4f) >= round_up_f((T)4 * R2)) continue;
+                const unsigned sbeg = __shfl_sync(FULL, nbeg, t), scnt = __shfl_sync(FULL, ncnt, t);
                 T brx = 0, bry = 0, brz = 0, br2 = (T)INFINITY;
+                seedj = 0xFFFFFFFFu;
                 for (unsigned q = lane; q < scnt; q += 32) {
                     const uint32_t j = sbeg + q;
                     T rx, ry, rz, r2;
@@ -1217,6 +1246,10 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 const bool has = seedj != 0xFFFFFFFFu;
                 const int32_t bcid = has ? (int32_t)(P.sorted[seedj] - pt_base) : 0;
                 status = run_window(has, brx, bry, brz, br2, seedj, bcid);
+                // the bin as lane 0's range (window lane = position mod 32)
+                if (status == ST_OK) status = process(sbeg, lane == 0 ? scnt : 0u, 0u, 0u);
+                seedj = 0xFFFFFFFFu;
+                done |= 1u << t;
             }
         }
     }
