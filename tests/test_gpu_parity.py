@@ -92,6 +92,23 @@ def test_celery_bit_exact(tess, oracle_mod, n, lo, hi):
     assert np.array_equal(dl, r.delimiters())
 
 
+def test_celery_crowded_bins(tess, oracle_mod):
+    """Bins of hundreds and of ~5,000 points (sorted by the whole block, in
+    shared and in global memory): the same sorted order as the oracle's."""
+    rng = np.random.default_rng(21)
+    pts = np.vstack([0.5 + 1e-3 * rng.random((5000, 3)), 0.2 + 0.05 * rng.random((2000, 3)),
+                     rng.random((1000, 3))])
+    pts = pts[rng.permutation(len(pts))]
+    with tess.Diagram(pts) as d:
+        cells, srt, dl = d.celery()
+    r = oracle_mod.Diagram(pts)
+    counts = np.diff(r.delimiters())
+    assert counts.max() > 4096 and ((counts > 32) & (counts <= 4096)).any()
+    assert np.array_equal(cells, r.bins())
+    assert np.array_equal(srt, r.sorted_indices())
+    assert np.array_equal(dl, r.delimiters())
+
+
 def test_oblong_and_offset_boxes(tess, oracle_mod):
     rng = np.random.default_rng(7)
     lo, hi = np.array([-5.0, 12.0, -10000.0]), np.array([-4.0, 1000.0, 1.0])

@@ -200,21 +200,89 @@ __global__ void k_scatter(GridBuffers g) {
     g.sorted[g.delims[g.bin[i]] + g.rank[i]] = i;
 }
 
-// Within-bin order ascending by input index (deterministic; the reference's
-// sort_unstable_by leaves it unspecified).  Bins hold ~1.25 points.
-__global__ void k_bin_order(GridBuffers g) {
-    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= g.total_bins) return;
-    const uint32_t beg = g.delims[b], end = g.delims[b + 1];
-    if (end - beg < 2) return;
-    for (uint32_t s = beg + 1; s < end; ++s) {
-        uint32_t v = g.sorted[s];
-        uint32_t t = s;
-        while (t > beg && g.sorted[t - 1] > v) {
-            g.sorted[t] = g.sorted[t - 1];
-            --t;
+// Ascending sort of a[0, n) by one block: a bitonic network in the form whose
+// comparators all point the same way (the first step of each merge compares
+// mirrored positions), over n rounded up to a power of two.  Positions >= n
+// stand for +inf: a comparator with one of them never swaps, so they are
+// simply skipped and never stored.  a is shared or global memory; the block's
+// barriers order the steps either way.
+// I is the index type: 32-bit in shared memory, 64-bit for a bin that may
+// approach 2^32 points.
+template <typename I>
+__device__ void block_bitonic_sort(uint32_t* a, I n) {
+    I np = 1;
+    while (np < n) np <<= 1;
+    const I half = np >> 1;
+    auto cmpswap = [&](I lo, I hi) {
+        if (hi < n) {
+            const uint32_t x = a[lo], y = a[hi];
+            if (x > y) {
+                a[lo] = y;
+                a[hi] = x;
+            }
         }
-        g.sorted[t] = v;
+    };
+    for (I k = 2; k <= np; k <<= 1) {
+        const I hk = k >> 1;
+        for (I i = threadIdx.x; i < half; i += blockDim.x) {
+            const I base = (i / hk) * k, off = i % hk;
+            cmpswap(base + off, base + k - 1 - off);
+        }
+        __syncthreads();
+        for (I j = hk >> 1; j > 0; j >>= 1) {
+            for (I i = threadIdx.x; i < half; i += blockDim.x) {
+                const I lo = (i / j) * 2 * j + i % j;
+                cmpswap(lo, lo + j);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Within-bin order ascending by input index (deterministic; the reference's
+// sort_unstable_by leaves it unspecified).  Bins hold ~1.25 points on
+// average: a thread per bin sorts the small ones by insertion; bins of more
+// than 32 points (crowded regions) are sorted afterwards by the whole block,
+// in shared memory up to kSortSmem points, in place beyond.
+constexpr uint32_t kSortSmem = 4096;
+__global__ void __launch_bounds__(256) k_bin_order(GridBuffers g) {
+    __shared__ uint32_t big[256];
+    __shared__ uint32_t nbig;
+    __shared__ uint32_t buf[kSortSmem];
+    if (threadIdx.x == 0) nbig = 0;
+    __syncthreads();
+    const uint64_t b0 = (uint64_t)blockIdx.x * blockDim.x;
+    const uint64_t b = b0 + threadIdx.x;
+    if (b < g.total_bins) {
+        const uint32_t beg = g.delims[b], end = g.delims[b + 1];
+        if (end - beg > 32) {
+            big[atomicAdd(&nbig, 1u)] = threadIdx.x;
+        } else if (end - beg >= 2) {
+            for (uint32_t s = beg + 1; s < end; ++s) {
+                uint32_t v = g.sorted[s];
+                uint32_t t = s;
+                while (t > beg && g.sorted[t - 1] > v) {
+                    g.sorted[t] = g.sorted[t - 1];
+                    --t;
+                }
+                g.sorted[t] = v;
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t nb = nbig;
+    for (uint32_t q = 0; q < nb; ++q) {
+        const uint64_t bb = b0 + big[q];
+        const uint32_t beg = g.delims[bb], n = g.delims[bb + 1] - beg;
+        if (n <= kSortSmem) {
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) buf[i] = g.sorted[beg + i];
+            __syncthreads();
+            block_bitonic_sort<uint32_t>(buf, n);
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) g.sorted[beg + i] = buf[i];
+        } else {
+            block_bitonic_sort<uint64_t>(g.sorted + beg, (uint64_t)n);
+        }
+        __syncthreads();
     }
 }
 
