@@ -49,10 +49,10 @@ RADIUS_METRIC = "radius queries/sec on 1 GB300 (find_neighbors_in_real_radius, F
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
 # captures of the same kernels on GB300.  The clipping pass was captured at
-# 1,000,000 cells (75.5 MB read + 169.6 MB written) and is scaled by cells: its
+# 1,000,000 cells (74.7 MB read + 169.2 MB written) and is scaled by cells: its
 # traffic is its output plus L2 misses, both per cell.  The radius passes were
 # captured at full size (16,777,216 queries, radius 0.006).
-NCU_CLIP_BYTES_PER_CELL = (75.547648e6 + 169.617408e6) / 1_000_000
+NCU_CLIP_BYTES_PER_CELL = (74.728448e6 + 169.210368e6) / 1_000_000
 NCU_RADIUS_BYTES = {"count": 3.846207488e9 + 0.50285184e9, "fill": 6.337812736e9 + 1.53743616e9}
 
 
