@@ -53,6 +53,9 @@ RADIUS_METRIC = "radius queries/sec on 1 GB300 (find_neighbors_in_real_radius, F
 # traffic is its output plus L2 misses, both per cell.  The radius passes were
 # captured at full size (16,777,216 queries, radius 0.006).
 NCU_CLIP_BYTES_PER_CELL = (74.728448e6 + 169.210368e6) / 1_000_000
+# Warp instructions of the same capture (smsp__inst_executed.sum), per cell: the
+# kernel is bound by instruction issue, so this gives its issue roofline.
+NCU_CLIP_INST_PER_CELL = 13_133_793_392 / 1_000_000
 NCU_RADIUS_BYTES = {"count": 3.846207488e9 + 0.50285184e9, "fill": 6.337812736e9 + 1.53743616e9}
 
 
@@ -365,6 +368,17 @@ def run_ours(args, ws, rank, local):
                 "traffic_source": "ncu DRAM bytes at 1,000,000 cells, scaled by cells",
                 "flops_per_cell": fpc,
                 "peak_source": f"nominal: {nsm} SMs x 128 FP32 lanes x 2 x {sm_mhz:.0f} MHz (sampled SM clock)",
+            }
+            # issue roofline: warp instructions per second against one instruction
+            # per cycle per scheduler (4 per SM)
+            iach = NCU_CLIP_INST_PER_CELL * n / (np.mean(clip_ms) / 1e3) / 1e12
+            ipeak = nsm * 4 * sm_mhz * 1e6 / 1e12
+            out["roofline_issue"] = {
+                "kernel": "k_clip<float,2,lean> (first clipping pass)", "bound": "issue", "achieved": iach,
+                "peak": ipeak, "unit": "T warp-instructions/s", "frac": iach / ipeak,
+                "instructions_per_cell": NCU_CLIP_INST_PER_CELL,
+                "source": "ncu smsp__inst_executed.sum at 1,000,000 cells, scaled by cells; peak = "
+                          f"{nsm} SMs x 4 schedulers x {sm_mhz:.0f} MHz",
             }
             nbins = obj.grid()[0] ** 3
             gbytes = (24 + 24 + 4) * n + 8 * nbins
