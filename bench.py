@@ -337,9 +337,11 @@ def run_ours(args, ws, rank, local):
     out = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32" if prec == "fp32" else "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload]["desc"], "cells": n, "precision":
-                   "FP32 + FP64 guard re-run" if prec == "fp32" else "FP64", "parallelism": "replicas",
+                   {"fp32": "FP32 + FP64 guard re-run", "fp64": "FP64",
+                    "mixed": "FP32 + FP64 guard re-run, FP64-accurate finish (two FP64-residual Newton steps "
+                             "per vertex, FP64 areas and volumes)"}[prec], "parallelism": "replicas",
                    "l2": l2_note(pts.nbytes, 12 * n * 15.5),
                    "step": "bin + clip + re-runs + CSR compaction, inputs resident in HBM"},
         "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
@@ -583,7 +585,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=list(WORKLOADS), default="uniform16m")
-    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--precision", choices=["fp32", "fp64", "mixed"], default="fp32")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--points", type=int, default=None,

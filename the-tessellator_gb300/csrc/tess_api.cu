@@ -180,7 +180,7 @@ struct Engine {
     uint64_t launches = 0;    // kernels launched so far (all passes)
     cudaGraphExec_t graph = nullptr;
     int graph_precision = -1;
-    int blocks_cache[2][4][3] = {};
+    int blocks_cache[2][4][8] = {};   // [kernel type][slots][form, with the exact flag]
 
     ~Engine() { release(); }
 
@@ -474,7 +474,9 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
     };
     uint32_t* const* L = E.d_list;
     if (timing) CU(cudaEventRecord(ev[0], E.stream));
-    if (precision == TESS_PRECISION_FP32_GUARD) {
+    if (precision == TESS_PRECISION_FP32_GUARD || precision == TESS_PRECISION_MIXED) {
+        // with the exact flag (MIXED) every FP32 pass finishes in FP64
+        const int X = precision == TESS_PRECISION_MIXED ? kFormExact : 0;
         // FP32: the lean first pass (2 slots per lane) over every cell but
         // those of crowded bins, which run seeded in the standard form;
         // capacity re-runs at 4 and 8 slots; the flagged cells re-run in the
@@ -484,18 +486,21 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         // (with TESS_FLAG_COUNTERS the first pass runs in the standard form:
         // the lean form keeps no counters)
         const bool lean = s0 <= 2 && !(E.cfg.flags & TESS_FLAG_COUNTERS);
-        TRY(pass(1, s0, lean ? kFormLean : kFormStd, nullptr, nullptr, L[L_FP64], cnt + L_FP64,
+        TRY(pass(1, s0, (lean ? kFormLean : kFormStd) | X, nullptr, nullptr, L[L_FP64], cnt + L_FP64,
                  one ? L[L_CAP1] : nullptr, cnt + L_CAP1, lean ? L[L_DENSE] : nullptr, cnt + L_DENSE));
         if (lean)
-            TRY(pass(1, 2, kFormStd, L[L_DENSE], cnt + L_DENSE, L[L_FP64], cnt + L_FP64, L[L_CAP1], cnt + L_CAP1));
+            TRY(pass(1, 2, kFormStd | X, L[L_DENSE], cnt + L_DENSE, L[L_FP64], cnt + L_FP64, L[L_CAP1],
+                     cnt + L_CAP1));
         if (timing) CU(cudaEventRecord(ev[1], E.stream));
         if (one) {
             const int s1 = two ? 4 : 8;
-            TRY(pass(1, s1, kFormStd, L[L_CAP1], cnt + L_CAP1, L[L_FP64], cnt + L_FP64, two ? L[L_CAP2] : nullptr,
+            TRY(pass(1, s1, kFormStd | X, L[L_CAP1], cnt + L_CAP1, L[L_FP64], cnt + L_FP64, two ? L[L_CAP2] : nullptr,
                      cnt + L_CAP2));
-            if (two) TRY(pass(1, 8, kFormStd, L[L_CAP2], cnt + L_CAP2, L[L_FP64], cnt + L_FP64, nullptr, nullptr));
+            if (two)
+                TRY(pass(1, 8, kFormStd | X, L[L_CAP2], cnt + L_CAP2, L[L_FP64], cnt + L_FP64, nullptr, nullptr));
         }
-        TRY(pass(1, 2, kFormHybrid, L[L_FP64], cnt + L_FP64, L[L_FP64B], cnt + L_FP64B, L[L_FP64B], cnt + L_FP64B));
+        TRY(pass(1, 2, kFormHybrid | X, L[L_FP64], cnt + L_FP64, L[L_FP64B], cnt + L_FP64B, L[L_FP64B],
+                 cnt + L_FP64B));
         TRY(pass(0, 2, kFormStd, L[L_FP64B], cnt + L_FP64B, nullptr, nullptr, L[L_CAP64A], cnt + L_CAP64A));
         TRY(pass(0, 4, kFormStd, L[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, L[L_CAP64B], cnt + L_CAP64B));
         TRY(pass(0, 8, kFormStd, L[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
@@ -516,7 +521,8 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
 
 tess_status engine_compute(Engine& E, int precision, double radius, int64_t group) {
     if (!E.built) return fail(TESS_E_STATE, "diagram is not built");
-    if (precision != TESS_PRECISION_FP64 && precision != TESS_PRECISION_FP32_GUARD)
+    if (precision != TESS_PRECISION_FP64 && precision != TESS_PRECISION_FP32_GUARD &&
+        precision != TESS_PRECISION_MIXED)
         return fail(TESS_E_INVALID, "unknown precision %d", precision);
     if (std::isnan(radius)) return fail(TESS_E_INVALID, "search_radius is NaN");
     CU(cudaSetDevice(E.device));
@@ -549,7 +555,7 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
         }
         E.stats.cells = E.total;
         E.stats.faces = used;
-        if (precision == TESS_PRECISION_FP32_GUARD) {
+        if (precision != TESS_PRECISION_FP64) {
             E.stats.rerun_fp64 = counts[L_FP64];
             E.stats.rerun_fp64_full = counts[L_FP64B];
             E.stats.dense_cells = counts[L_DENSE];
@@ -1164,7 +1170,8 @@ static tess_status single_cell(tess_diagram* d, const size_t* i, const double* p
     if (!d->E.built) return fail(TESS_E_STATE, "diagram is not built");
     if ((lo == nullptr) != (hi == nullptr)) return fail(TESS_E_INVALID, "give both lo and hi, or neither");
     if (lo) TRY(validate_box(lo, hi));
-    if ((int)precision != TESS_PRECISION_FP64 && (int)precision != TESS_PRECISION_FP32_GUARD)
+    if ((int)precision != TESS_PRECISION_FP64 && (int)precision != TESS_PRECISION_FP32_GUARD &&
+        (int)precision != TESS_PRECISION_MIXED)
         return fail(TESS_E_INVALID, "unknown precision %d", (int)precision);
     if (std::isnan(search_radius)) return fail(TESS_E_INVALID, "search_radius is NaN");
     uint32_t gs = 0;
@@ -1307,13 +1314,15 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
     if (!b) return fail(TESS_E_INVALID, "batch is NULL");
     Engine& E = b->E;
     const int prec = (int)precision;
-    if (prec != TESS_PRECISION_FP64 && prec != TESS_PRECISION_FP32_GUARD)
+    if (prec != TESS_PRECISION_FP64 && prec != TESS_PRECISION_FP32_GUARD && prec != TESS_PRECISION_MIXED)
         return fail(TESS_E_INVALID, "unknown precision %d", prec);
     CU(cudaSetDevice(E.device));
     if (!E.graph || E.graph_precision != prec) {
         // warm the per-kernel attributes and occupancy queries outside capture
         for (int pr : {0, 1})
-            for (int s : {2, 4, 8}) E.blocks(pr, s);
+            for (int s : {2, 4, 8})
+                for (int f : {(int)kFormLean, (int)kFormStd, (int)kFormHybrid})
+                    for (int x : {0, (int)kFormExact}) E.blocks(pr, s, f | x);
         if (E.graph) cudaGraphExecDestroy(E.graph);
         E.graph = nullptr;
         cudaGraph_t g = nullptr;
@@ -1341,7 +1350,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
         CU(cudaEventRecord(e0, E.stream));
     }
     CU(cudaGraphLaunch(E.graph, E.stream));
-    E.launches += kGridLaunches + (prec == 1 ? 7 : 3);
+    E.launches += kGridLaunches + (prec != TESS_PRECISION_FP64 ? 7 : 3);
     if (timing) CU(cudaEventRecord(e1, E.stream));
     unsigned long long used = 0;
     unsigned counts[16];
@@ -1369,9 +1378,10 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
     }
     E.stats.cells = E.total;
     E.stats.faces = used;
-    E.stats.rerun_fp64 = prec == 1 ? counts[L_FP64] : 0;
-    E.stats.rerun_fp64_full = prec == 1 ? counts[L_FP64B] : 0;
-    E.stats.dense_cells = prec == 1 ? counts[L_DENSE] : 0;
+    const bool f32 = prec != TESS_PRECISION_FP64;
+    E.stats.rerun_fp64 = f32 ? counts[L_FP64] : 0;
+    E.stats.rerun_fp64_full = f32 ? counts[L_FP64B] : 0;
+    E.stats.dense_cells = f32 ? counts[L_DENSE] : 0;
     E.stats.rerun_capacity = (uint64_t)counts[L_CAP1] + counts[L_CAP2] + counts[L_CAP64A] + counts[L_CAP64B];
     E.stats.failed = counts[L_FAIL];
     E.stats.rerun_guard = counts[L_REASON + ST_GUARD];

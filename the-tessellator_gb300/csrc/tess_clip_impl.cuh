@@ -115,6 +115,7 @@ struct Smem {
             double qx[PF], qy[PF], qz[PF], qh[PF];
             float fqx[PF], fqy[PF], fqz[PF], qdist[PF];
             float dx[VF], dy[VF], dz[VF];
+            float ex[VF], ey[VF], ez[VF];     // exact form: second correction
             uint32_t fdeg[P];                 // live vertices per face
             int32_t flist[P];                 // compacted face ids
             uint8_t fsta[P];                  // one vertex of each face
@@ -858,9 +859,11 @@ template <typename T, int K, bool GEO, int FORM>
 __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int lane, Work& W) {
     using S_t = Smem<T, K>;
     constexpr bool GUARD = sizeof(T) == 4;
+    constexpr int BASE = FORM & 3;                                  // lean, std or hybrid
+    constexpr bool EXACT = GUARD && (FORM & kFormExact) != 0;       // FP64-accurate finalize
     // the lean first pass sends crowded cells to a seeded pass instead (the
     // seeding code would cost its hot loop registers)
-    constexpr bool kSeedForm = FORM != kFormLean;
+    constexpr bool kSeedForm = BASE != kFormLean;
     // ---- diagram of this cell ----
     int d = 0;
     if (P.ndiag > 1 && !P.at_point) {
@@ -1018,7 +1021,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         // nothing later (the cell only shrinks), so only possible cutters
         // (and guard-band cases, which the serial test reports) go on to
         // the serial nearest-first loop.  Same arithmetic as cut().
-        if (FORM != kFormLean && __popc(km) >= kPretestMin) {
+        if (BASE != kFormLean && __popc(km) >= kPretestMin) {
             bool maycut = false;
             if (keep) {
                 T nx_, ny_, nz_, off_, rn_;
@@ -1063,12 +1066,12 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             }
             T nx, ny, nz, off, rn;
             bisector(cx, cy, cz, c2, nx, ny, nz, off, rn);
-            const int r = cut<T, K, GUARD, FORM == kFormHybrid>(S, C, nx, ny, nz, off, rn, cR, eC, cidb, cj, lane,
+            const int r = cut<T, K, GUARD, BASE == kFormHybrid>(S, C, nx, ny, nz, off, rn, cR, eC, cidb, cj, lane,
                                                                    P, fsite);
-            if constexpr (FORM != kFormLean) ++W.tested;
+            if constexpr (BASE != kFormLean) ++W.tested;
             if (r < 0) return -r;
             if (r > 0) {
-                if constexpr (FORM != kFormLean) {
+                if constexpr (BASE != kFormLean) {
                     ++W.cuts;
                     W.newv += (unsigned)(r - 1);
                 }
@@ -1079,7 +1082,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 // (convexity), so a radius that grew (or is no longer
                 // finite) means an FP32 vertex went wrong after an
                 // FP64-decided test; the cell re-runs in FP64
-                if (FORM == kFormHybrid && !(R2 <= R2b * (T)1.001)) return ST_GUARD;
+                if (BASE == kFormHybrid && !(R2 <= R2b * (T)1.001)) return ST_GUARD;
             }
         }
         return ST_OK;
@@ -1100,7 +1103,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         S.cbeg2[lane] = begB;
         __syncwarp();
         for (unsigned w0 = 0; w0 < total; w0 += 32) {
-            if constexpr (FORM != kFormLean) ++W.windows;
+            if constexpr (BASE != kFormLean) ++W.windows;
             const unsigned c = w0 + lane;
             bool keep = false;
             T rx = 0, ry = 0, rz = 0, r2 = 0;
@@ -1261,7 +1264,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     if (kBatch2) load_entry(32 + lane, eb);
     // lean first pass: a crowded own bin (table entry 0, lane 0's first
     // entry) sends the cell to the seeded pass
-    if (FORM == kFormLean && P.list_dense && __shfl_sync(FULL, ea.cnt, 0) >= kSeedMin) status = ST_DENSE;
+    if (BASE == kFormLean && P.list_dense && __shfl_sync(FULL, ea.cnt, 0) >= kSeedMin) status = ST_DENSE;
     while (status == ST_OK) {
         // The table key is rounded toward zero and the threshold up, so
         // stopping on key >= thr never drops a bin that could hold a cutter.
@@ -1283,7 +1286,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             load_entry(t + lane, ea);
             if (kBatch2) load_entry(t + 32 + lane, eb);
         }
-        if constexpr (FORM != kFormLean) ++W.batches;
+        if constexpr (BASE != kFormLean) ++W.batches;
         status = process(ba, ca, bb, cb);
         if (status != ST_OK) break;
         if (!kPrefetch && !last) {
@@ -1315,7 +1318,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     if (key > D.tab_kmax && key < thr && !(radius >= 0.0 && key > radius)) lb = bin_of(i, j, k);
                 }
                 if (!__any_sync(FULL, lb >= 0)) continue;
-                if constexpr (FORM != kFormLean) ++W.batches;
+                if constexpr (BASE != kFormLean) ++W.batches;
                 unsigned beg = 0, cnt = 0;
                 if (lb >= 0) {
                     beg = P.delims[lb];
@@ -1431,6 +1434,18 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     S.dx[s] = ddx;
                     S.dy[s] = ddy;
                     S.dz[s] = ddz;
+                    if constexpr (EXACT) {
+                        // a second step from x + d (exact in FP64): its residuals
+                        // are ~1e-7 of the first, so the FP32 solve leaves an error
+                        // at the FP64 rounding of the residuals
+                        const double x1 = x + (double)ddx, y1 = y + (double)ddy, z1 = z + (double)ddz;
+                        const float sa_ = (float)(S.qh[a] - (S.qx[a] * x1 + S.qy[a] * y1 + S.qz[a] * z1));
+                        const float sb_ = (float)(S.qh[b] - (S.qx[b] * x1 + S.qy[b] * y1 + S.qz[b] * z1));
+                        const float sc_ = (float)(S.qh[c] - (S.qx[c] * x1 + S.qy[c] * y1 + S.qz[c] * z1));
+                        S.ex[s] = (sa_ * bcx + sb_ * cax + sc_ * abx) * inv;
+                        S.ey[s] = (sa_ * bcy + sb_ * cay + sc_ * aby) * inv;
+                        S.ez[s] = (sa_ * bcz + sb_ * caz + sc_ * abz) * inv;
+                    }
                 }
             }
             __syncwarp();
@@ -1443,7 +1458,49 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             if (p < C.np && S.fdeg[p] > 0) {
                 const int start = S.fsta[p];
                 int cur = start, steps = 0;
-                if constexpr (GUARD) {
+                if constexpr (EXACT) {
+                    // Fan from the first vertex (weighted_normal,
+                    // polyhedron.rs:776-808) in FP64 on the twice-refined
+                    // positions x32 + d + e, face-relative; the volume as
+                    // anchor . (2 area n) / 6 (compute_volume, polyhedron.rs:838-855).
+                    auto rel = [&](int q, double& X, double& Y, double& Z) {
+                        X = ((double)S.vx[q] - (double)S.vx[start]) + ((double)S.dx[q] - (double)S.dx[start]) +
+                            ((double)S.ex[q] - (double)S.ex[start]);
+                        Y = ((double)S.vy[q] - (double)S.vy[start]) + ((double)S.dy[q] - (double)S.dy[start]) +
+                            ((double)S.ey[q] - (double)S.ey[start]);
+                        Z = ((double)S.vz[q] - (double)S.vz[start]) + ((double)S.dz[q] - (double)S.dz[start]) +
+                            ((double)S.ez[q] - (double)S.ez[start]);
+                    };
+                    double ux = 0.0, uy = 0.0, uz = 0.0, wx = 0.0, wy = 0.0, wz = 0.0;
+                    do {
+                        const uint32_t tt = S.tri[cur], aa = S.adj[cur];
+                        const int i = plane_of(tt, 0) == p ? 0 : (plane_of(tt, 1) == p ? 1 : 2);
+                        const int nx = plane_of(aa, i);
+                        if (plane_of(tt, i) != p || nx >= S_t::V) {
+                            bad = true;
+                            break;
+                        }
+                        double vx_, vy_, vz_;
+                        rel(nx, vx_, vy_, vz_);
+                        if (steps > 0) {
+                            // the walk runs clockwise seen from outside:
+                            // next x current is outward
+                            wx += vy_ * uz - vz_ * uy;
+                            wy += vz_ * ux - vx_ * uz;
+                            wz += vx_ * uy - vy_ * ux;
+                        }
+                        ux = vx_;
+                        uy = vy_;
+                        uz = vz_;
+                        cur = nx;
+                        ++steps;
+                    } while (cur != start && steps <= S_t::V);
+                    const double A0 = ((double)S.vx[start] + (double)S.dx[start]) + (double)S.ex[start];
+                    const double A1 = ((double)S.vy[start] + (double)S.dy[start]) + (double)S.ey[start];
+                    const double A2 = ((double)S.vz[start] + (double)S.dz[start]) + (double)S.ez[start];
+                    farea[r] = 0.5 * sqrt(wx * wx + wy * wy + wz * wz);
+                    vpart += (A0 * wx + A1 * wy + A2 * wz) * 0.5;
+                } else if constexpr (GUARD) {
                     // Fan from the first vertex (weighted_normal,
                     // polyhedron.rs:776-808) on refined positions:
                     // (x - anchor) = (x32 - a32) + (dx - da), in FP32.
@@ -1504,7 +1561,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         }
         // volume: sum of pyramids from the site, area * height / 3
         // (compute_volume, polyhedron.rs:838-855)
-        vol = GUARD ? warp_sum_d(vpart) * (1.0 / 3.0) : warp_sum_d(vpart) / 3.0;
+        vol = (GUARD && !EXACT) ? warp_sum_d(vpart) * (1.0 / 3.0) : warp_sum_d(vpart) / 3.0;
 #pragma unroll
         for (int r = 0; r < R; ++r) F += __popc(__ballot_sync(FULL, fdegr[r] > 0));
         // Every vertex has three faces: V - E + F = 2 with E = 3V/2.

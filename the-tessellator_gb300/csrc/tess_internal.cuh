@@ -275,7 +275,10 @@ struct ClipParams {
 //                first pass flagged: a plane test in the guard band is
 //                decided in FP64 for the vertices concerned (each recomputed
 //                from its three planes) instead of re-running the cell.
-enum ClipForm : int { kFormLean = 0, kFormStd = 1, kFormHybrid = 2 };
+//   kFormExact   a flag on the FP32 forms: the finalize refines every vertex
+//                with a second FP64-residual Newton step and accumulates face
+//                areas and the volume in FP64 (FP64-accurate results)
+enum ClipForm : int { kFormLean = 0, kFormStd = 1, kFormHybrid = 2, kFormExact = 4 };
 cudaError_t launch_clip_f32(const ClipParams& p, int slots, int form, int wpb, int blocks, cudaStream_t s);
 cudaError_t launch_clip_f64(const ClipParams& p, int slots, int form, int wpb, int blocks, cudaStream_t s);
 int clip_blocks_f32(int slots, int form, int wpb, int device);

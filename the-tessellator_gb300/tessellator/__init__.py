@@ -30,22 +30,26 @@ from typing import List, Optional
 
 import numpy as np
 
-from ._capi import (FLAG_COUNTERS, FLAG_TIMING, PRECISION_FP32_GUARD, PRECISION_FP64, CellGeometry, Config, Stats,
-                    TessError, check, default_config, last_error, lib)
+from ._capi import (FLAG_COUNTERS, FLAG_TIMING, PRECISION_FP32_GUARD, PRECISION_FP64, PRECISION_MIXED,
+                    CellGeometry, Config, Stats, TessError, check, default_config, last_error, lib)
 
 __all__ = ["Polyhedron", "Diagram", "Cell", "VoronoiFace", "Batch", "TessError", "Config",
-           "default_config", "PRECISION_FP64", "PRECISION_FP32_GUARD", "FLAG_TIMING", "FLAG_COUNTERS", "lib",
+           "default_config", "PRECISION_FP64", "PRECISION_FP32_GUARD", "PRECISION_MIXED", "FLAG_TIMING",
+           "FLAG_COUNTERS", "lib",
            "last_error"]
 
+# "mixed": the FP32 + guard clipping with an FP64-accurate finish (FP64-grade
+# results, see TESS_PRECISION_MIXED)
 _PREC = {"fp64": PRECISION_FP64, "fp32": PRECISION_FP32_GUARD, "fp32_guard": PRECISION_FP32_GUARD,
-         PRECISION_FP64: PRECISION_FP64, PRECISION_FP32_GUARD: PRECISION_FP32_GUARD}
+         "mixed": PRECISION_MIXED, PRECISION_FP64: PRECISION_FP64, PRECISION_FP32_GUARD: PRECISION_FP32_GUARD,
+         PRECISION_MIXED: PRECISION_MIXED}
 
 
 def _prec(p) -> int:
     try:
         return _PREC[p]
     except KeyError:
-        raise ValueError(f"unknown precision {p!r} (use 'fp64' or 'fp32')") from None
+        raise ValueError(f"unknown precision {p!r} (use 'fp64', 'fp32' or 'mixed')") from None
 
 
 def _dp(a: np.ndarray):
