@@ -115,7 +115,7 @@ struct Smem {
             double qx[PF], qy[PF], qz[PF], qh[PF];
             float fqx[PF], fqy[PF], fqz[PF], qdist[PF];
             float dx[VF], dy[VF], dz[VF];
-            float ex[VF], ey[VF], ez[VF];     // exact form: second correction
+            double rx[VF], ry[VF], rz[VF];    // exact form: refined FP64 positions
             uint32_t fdeg[P];                 // live vertices per face
             int32_t flist[P];                 // compacted face ids
             uint8_t fsta[P];                  // one vertex of each face
@@ -1442,9 +1442,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                         const float sa_ = (float)(S.qh[a] - (S.qx[a] * x1 + S.qy[a] * y1 + S.qz[a] * z1));
                         const float sb_ = (float)(S.qh[b] - (S.qx[b] * x1 + S.qy[b] * y1 + S.qz[b] * z1));
                         const float sc_ = (float)(S.qh[c] - (S.qx[c] * x1 + S.qy[c] * y1 + S.qz[c] * z1));
-                        S.ex[s] = (sa_ * bcx + sb_ * cax + sc_ * abx) * inv;
-                        S.ey[s] = (sa_ * bcy + sb_ * cay + sc_ * aby) * inv;
-                        S.ez[s] = (sa_ * bcz + sb_ * caz + sc_ * abz) * inv;
+                        S.rx[s] = x1 + (double)((sa_ * bcx + sb_ * cax + sc_ * abx) * inv);
+                        S.ry[s] = y1 + (double)((sa_ * bcy + sb_ * cay + sc_ * aby) * inv);
+                        S.rz[s] = z1 + (double)((sa_ * bcz + sb_ * caz + sc_ * abz) * inv);
                     }
                 }
             }
@@ -1459,19 +1459,20 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 const int start = S.fsta[p];
                 int cur = start, steps = 0;
                 if constexpr (EXACT) {
-                    // Fan from the first vertex (weighted_normal,
-                    // polyhedron.rs:776-808) in FP64 on the twice-refined
-                    // positions x32 + d + e, face-relative; the volume as
-                    // anchor . (2 area n) / 6 (compute_volume, polyhedron.rs:838-855).
-                    auto rel = [&](int q, double& X, double& Y, double& Z) {
-                        X = ((double)S.vx[q] - (double)S.vx[start]) + ((double)S.dx[q] - (double)S.dx[start]) +
-                            ((double)S.ex[q] - (double)S.ex[start]);
-                        Y = ((double)S.vy[q] - (double)S.vy[start]) + ((double)S.dy[q] - (double)S.dy[start]) +
-                            ((double)S.ey[q] - (double)S.ey[start]);
-                        Z = ((double)S.vz[q] - (double)S.vz[start]) + ((double)S.dz[q] - (double)S.dz[start]) +
-                            ((double)S.ez[q] - (double)S.ez[start]);
-                    };
-                    double ux = 0.0, uy = 0.0, uz = 0.0, wx = 0.0, wy = 0.0, wz = 0.0;
+                    // The face's area from its projection on the plane normal
+                    // to the dominant axis m of its normal q (shoelace on the
+                    // refined FP64 positions, face-relative): w_m = 2 A q_m/|q|
+                    // (walk clockwise seen from outside: next x current is
+                    // outward).  Area = w_m |q| / (2 q_m); the pyramid from the
+                    // site, h A / 3 with h = qh / |q|, is qh w_m / (6 q_m)
+                    // (compute_volume, polyhedron.rs:838-855).
+                    const double q0 = S.qx[p], q1 = S.qy[p], q2 = S.qz[p];
+                    const int m = (fabs(q0) >= fabs(q1) && fabs(q0) >= fabs(q2)) ? 0 : (fabs(q1) >= fabs(q2) ? 1 : 2);
+                    const double* X1 = m == 0 ? S.ry : (m == 1 ? S.rz : S.rx);
+                    const double* X2 = m == 0 ? S.rz : (m == 1 ? S.rx : S.ry);
+                    const double qm = m == 0 ? q0 : (m == 1 ? q1 : q2);
+                    const double a1 = X1[start], a2 = X2[start];
+                    double u1 = 0.0, u2 = 0.0, wm = 0.0;
                     do {
                         const uint32_t tt = S.tri[cur], aa = S.adj[cur];
                         const int i = plane_of(tt, 0) == p ? 0 : (plane_of(tt, 1) == p ? 1 : 2);
@@ -1480,26 +1481,16 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                             bad = true;
                             break;
                         }
-                        double vx_, vy_, vz_;
-                        rel(nx, vx_, vy_, vz_);
-                        if (steps > 0) {
-                            // the walk runs clockwise seen from outside:
-                            // next x current is outward
-                            wx += vy_ * uz - vz_ * uy;
-                            wy += vz_ * ux - vx_ * uz;
-                            wz += vx_ * uy - vy_ * ux;
-                        }
-                        ux = vx_;
-                        uy = vy_;
-                        uz = vz_;
+                        const double v1 = X1[nx] - a1, v2 = X2[nx] - a2;
+                        if (steps > 0) wm += v1 * u2 - v2 * u1;
+                        u1 = v1;
+                        u2 = v2;
                         cur = nx;
                         ++steps;
                     } while (cur != start && steps <= S_t::V);
-                    const double A0 = ((double)S.vx[start] + (double)S.dx[start]) + (double)S.ex[start];
-                    const double A1 = ((double)S.vy[start] + (double)S.dy[start]) + (double)S.ey[start];
-                    const double A2 = ((double)S.vz[start] + (double)S.dz[start]) + (double)S.ez[start];
-                    farea[r] = 0.5 * sqrt(wx * wx + wy * wy + wz * wz);
-                    vpart += (A0 * wx + A1 * wy + A2 * wz) * 0.5;
+                    const double inv_qm = 1.0 / qm;
+                    farea[r] = 0.5 * wm * inv_qm * sqrt(q0 * q0 + q1 * q1 + q2 * q2);
+                    vpart += S.qh[p] * wm * inv_qm * 0.5;
                 } else if constexpr (GUARD) {
                     // Fan from the first vertex (weighted_normal,
                     // polyhedron.rs:776-808) on refined positions:
