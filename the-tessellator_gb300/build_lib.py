@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "tessellator", "libtessgpu.so")
 BUILD = os.path.join(ROOT, "_build", "tessgpu")
-SOURCES = ["tess_grid.cu", "tess_clip.cu", "tess_clip_f32.cu", "tess_clip_f64.cu", "tess_api.cu",
+SOURCES = ["tess_grid.cu", "tess_clip.cu", "tess_clip_f32.cu", "tess_clip_f32x.cu", "tess_clip_f64.cu", "tess_api.cu",
            "tess_noalloc.cu", "tess_radius.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
