@@ -43,8 +43,24 @@ def test_default_config(tess):
     c = tess.default_config()
     assert c.bin_density == 1.25          # celery.rs:185-188
     assert c.slots_per_lane == 2 and c.table_gaps == 8
-    assert 0 < c.guard_rel < 1e-3
+    assert c.guard_rel == 4e-7            # the FP32 test's rounding bound, 3e-7, with a third in hand
     assert c.stream is None and c.flags == 0
+
+
+@pytest.mark.parametrize("field,value", [("guard_rel", 1e-7), ("guard_rel", 0.0), ("guard_rel", float("nan")),
+                                         ("verify_rel", 0.0), ("bin_density", -1.0), ("slots_per_lane", 3)])
+def test_config_rejected(tess, field, value):
+    """Settings that would void the FP32 form's guarantees (or make no sense)
+    are refused before any device work."""
+    L = tess.lib()
+    c = tess.default_config()
+    setattr(c, field, value)
+    pts = np.random.default_rng(1).random((10, 3))
+    h = C.c_void_p()
+    st = L.tess_diagram_create(pts.ctypes.data_as(C.POINTER(C.c_double)), 10, None, None, None, C.byref(c),
+                               C.byref(h))
+    assert st == tess._capi.TESS_E_INVALID
+    assert field in tess.last_error()
 
 
 def test_argument_errors(tess):

@@ -236,7 +236,10 @@ tess_status check_config(const tess_config& c) {
     if (c.warps_per_block < 1 || c.warps_per_block > 32) return fail(TESS_E_INVALID, "warps_per_block must be in [1, 32]");
     if (c.slots_per_lane != 2 && c.slots_per_lane != 4 && c.slots_per_lane != 8)
         return fail(TESS_E_INVALID, "slots_per_lane must be 2, 4 or 8");
-    if (!(c.guard_rel >= 0.0) || !(c.guard_rel < 1.0)) return fail(TESS_E_INVALID, "guard_rel must be in [0, 1)");
+    // below 3e-7 the guard band no longer covers an FP32 plane test's rounding
+    if (!(c.guard_rel >= 3e-7) || !(c.guard_rel < 1e-2))
+        return fail(TESS_E_INVALID, "guard_rel must be in [3e-7, 1e-2)");
+    if (!(c.verify_rel > 0.0) || !(c.verify_rel < 1.0)) return fail(TESS_E_INVALID, "verify_rel must be in (0, 1)");
     return TESS_OK;
 }
 
