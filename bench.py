@@ -371,17 +371,18 @@ def run_ours(args, ws, rank, local):
                 "flops_per_cell": fpc,
                 "peak_source": f"nominal: {nsm} SMs x 128 FP32 lanes x 2 x {sm_mhz:.0f} MHz (sampled SM clock)",
             }
-            # issue roofline: warp instructions per second against one instruction
-            # per cycle per scheduler (4 per SM)
+            # issue roofline of the FP32 lean pass (its ncu instruction count):
+            # warp instructions per second against one per cycle per scheduler
             iach = NCU_CLIP_INST_PER_CELL * n / (np.mean(clip_ms) / 1e3) / 1e12
             ipeak = nsm * 4 * sm_mhz * 1e6 / 1e12
-            out["roofline_issue"] = {
-                "kernel": "k_clip<float,2,lean> (first clipping pass)", "bound": "issue", "achieved": iach,
-                "peak": ipeak, "unit": "T warp-instructions/s", "frac": iach / ipeak,
-                "instructions_per_cell": NCU_CLIP_INST_PER_CELL,
-                "source": "ncu smsp__inst_executed.sum at 1,000,000 cells, scaled by cells; peak = "
-                          f"{nsm} SMs x 4 schedulers x {sm_mhz:.0f} MHz",
-            }
+            if prec == "fp32":
+                out["roofline_issue"] = {
+                    "kernel": "k_clip<float,2,lean> (first clipping pass)", "bound": "issue", "achieved": iach,
+                    "peak": ipeak, "unit": "T warp-instructions/s", "frac": iach / ipeak,
+                    "instructions_per_cell": NCU_CLIP_INST_PER_CELL,
+                    "source": "ncu smsp__inst_executed.sum at 1,000,000 cells, scaled by cells; peak = "
+                              f"{nsm} SMs x 4 schedulers x {sm_mhz:.0f} MHz",
+                }
             nbins = obj.grid()[0] ** 3
             gbytes = (24 + 24 + 4) * n + 8 * nbins
             hbm = peaks.get("hbm_gbs", 6800.0)
