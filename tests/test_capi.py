@@ -34,6 +34,14 @@ def test_every_declared_function_is_exported(tess):
     assert sorted(tess._capi.EXPORTS) == decl
 
 
+def test_rust_binding_declares_every_function():
+    """The extern block a maintainer adds to the Rust crate names every
+    function of the header, and no other."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    rust = sorted(set(re.findall(r"\bpub fn (tess_[a-z_0-9]+)\s*\(", text)))
+    assert rust == declared_functions()
+
+
 def test_library_needs_no_gpu_to_load(tess):
     L = tess.lib()
     assert L.tess_version().startswith(b"tessellator-gb300")
