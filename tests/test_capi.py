@@ -119,3 +119,28 @@ def test_python_api_mirrors_interface_rs(tess):
     for name in ("compute_vertices", "compute_area", "compute_neighbor"):
         assert hasattr(tess.VoronoiFace, name)
     assert hasattr(tess.Polyhedron, "new")
+
+
+def c_struct_fields(name):
+    """Field names, in order, of `typedef struct {...} name;` in the header."""
+    text = open(os.path.join(ROOT, "include", "tessellator.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    body = re.search(r"typedef struct \{([^}]*)\}\s*" + name + r"\s*;", text, flags=re.S).group(1)
+    names = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if decl:
+            names.append(re.sub(r"\[.*?\]", "", decl).split()[-1].lstrip("*"))
+    return names
+
+
+@pytest.mark.parametrize("cname,pyname", [("tess_stats", "Stats"), ("tess_config", "Config")])
+def test_struct_layouts_agree(tess, cname, pyname):
+    """tess_stats and tess_config: the same fields in the same order in the
+    header, the Python mirror and the Rust binding."""
+    fields = c_struct_fields(cname)
+    assert [f for f, _ in getattr(tess._capi, pyname)._fields_] == fields
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    body = re.search(r"pub struct " + cname + r" \{(.*?)\}", text, flags=re.S).group(1)
+    assert re.findall(r"pub (\w+):", body) == fields
+
