@@ -160,7 +160,12 @@ class Diagram:
 
     def compute_all(self, precision="fp32", search_radius: Optional[float] = None,
                     target_group: Optional[int] = None) -> "Diagram":
-        """Every cell: get_cell_at_index(i, ...) + compute_voronoi_cell()."""
+        """Every cell: get_cell_at_index(i, ...) + compute_voronoi_cell().
+
+        ``precision``: "fp32" (FP32 clipping with guard bands and FP64 re-runs;
+        volumes to about 1e-7), "mixed" (the same clipping with an FP64-accurate
+        finish; volumes to 1e-12) or "fp64" (plain FP64).  Neighbour lists are
+        the same in all three."""
         check(lib().tess_diagram_compute_all(self._h, _prec(precision), _radius(search_radius),
                                              _group(target_group)))
         return self
@@ -425,6 +430,8 @@ class Batch:
                                   C.byref(cfg), C.byref(self._h)))
 
     def compute(self, precision="fp32") -> "Batch":
+        """Every cell of every diagram ("fp32", "mixed" or "fp64", as
+        Diagram.compute_all), in one CUDA-graph launch per precision."""
         check(lib().tess_batch_compute(self._h, _prec(precision)))
         return self
 
