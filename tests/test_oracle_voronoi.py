@@ -59,16 +59,24 @@ def test_qhull_live(oracle_mod):
     assert checked > 800
 
 
-@pytest.mark.parametrize("gen", ["uniform", "clustered"])
+@pytest.mark.parametrize("gen", ["uniform", "clustered", "crowded"])
 def test_secure_equals_brute_bit_exact(oracle_mod, gen):
     """The security-radius stop changes nothing: the same cuts happen in the
-    same order as the reference's walk over every point (celery.rs:971)."""
+    same order as the reference's walk over every point (celery.rs:971).
+    "crowded": bins of several hundred points, as in clustered inputs."""
     rng = np.random.default_rng(22)
     if gen == "uniform":
         pts = rng.random((1200, 3))
-    else:
+    elif gen == "clustered":
         c = 0.2 + 0.6 * rng.random((4, 3))
         pts = np.clip(c[rng.integers(0, 4, 1200)] + 0.03 * rng.standard_normal((1200, 3)), 0, 1)
+    else:
+        c = 0.2 + 0.6 * rng.random((3, 3))
+        pts = np.vstack([c[rng.integers(0, 3, 2400)] + 0.004 * rng.standard_normal((2400, 3)),
+                         rng.random((300, 3))])
+        pts = np.clip(pts, 0, 1)
+        counts = np.diff(oracle_mod.Diagram(pts).delimiters())
+        assert counts.max() >= 300
     d = oracle_mod.Diagram(pts, lo=[0, 0, 0], hi=[1, 1, 1])
     a = d.compute_all(mode=oracle_mod.MODE_SECURE)
     b = d.compute_all(mode=oracle_mod.MODE_BRUTE)
