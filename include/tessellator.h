@@ -307,6 +307,11 @@ tess_status tess_batch_create(size_t ndiag, const uint64_t* pt_offsets, const do
 /* Bin and clip every diagram.  The sequence of launches is captured in a CUDA
  * graph on first use and replayed afterwards. */
 tess_status tess_batch_compute(tess_batch* b, tess_precision precision);
+/* Replace every diagram's points (same offsets and boxes), from host memory or
+ * (on_device != 0) device memory; the next tess_batch_compute bins them
+ * again.  The batch form of Celery::reset (celery.rs:253-266) over
+ * tess_diagram_update_points. */
+tess_status tess_batch_update_points(tess_batch* b, const double* xyz, int on_device);
 tess_status tess_batch_stats(const tess_batch* b, tess_stats* out);
 /* Volumes of all points (concatenated order), host buffer. */
 tess_status tess_batch_volumes(tess_batch* b, double* volumes);

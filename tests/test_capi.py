@@ -34,12 +34,41 @@ def test_every_declared_function_is_exported(tess):
     assert sorted(tess._capi.EXPORTS) == decl
 
 
+RUST_FFI = os.path.join(ROOT, "rust", "src", "gpu_ffi.rs")
+RUST_API = os.path.join(ROOT, "rust", "src", "interface.rs")
+
+
 def test_rust_binding_declares_every_function():
-    """The extern block a maintainer adds to the Rust crate names every
-    function of the header, and no other."""
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    """The crate's extern block (rust/src/gpu_ffi.rs) names every function of
+    the header, and no other."""
+    text = open(RUST_FFI).read()
     rust = sorted(set(re.findall(r"\bpub fn (tess_[a-z_0-9]+)\s*\(", text)))
     assert rust == declared_functions()
+
+
+def test_rust_constants_match_the_header():
+    """Status codes and precisions in the crate equal the header's enums."""
+    header = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "tessellator.h")).read(), flags=re.S)
+    cvals = dict(re.findall(r"\b(TESS_(?:OK|E_[A-Z]+|PRECISION_[A-Z0-9_]+))\s*=\s*(\d+)", header))
+    rvals = dict(re.findall(r"pub const (TESS_(?:OK|E_[A-Z]+|PRECISION_[A-Z0-9_]+)):[^=]*=\s*(\d+)",
+                            open(RUST_FFI).read()))
+    assert len(cvals) >= 11
+    assert rvals == cvals
+
+
+def test_rust_wrapper_keeps_the_reference_names():
+    """The safe wrapper (rust/src/interface.rs) has the public methods of the
+    reference's interface.rs and calls only functions the binding declares."""
+    text = open(RUST_API).read()
+    for name in ("get_cell_at_index", "get_cell_at_particle", "compute_voronoi_cell", "compute_volume",
+                 "compute_neighbors", "compute_neighbor_cloud", "compute_vertices", "compute_faces",
+                 "original_index", "compute_area", "compute_neighbor", "compute_all", "volumes",
+                 "neighbors_csr", "find_neighbors_in_real_radius", "find_cells_in_radius"):
+        assert re.search(r"pub fn " + name + r"\b", text), name
+    called = set(re.findall(r"\b(tess_[a-z_0-9]+)\s*\(", text))
+    assert called and called <= set(declared_functions())
+    for f in ("Cargo.toml", "build.rs", os.path.join("src", "lib.rs")):
+        assert os.path.exists(os.path.join(ROOT, "rust", f)), f
 
 
 def test_library_needs_no_gpu_to_load(tess):
@@ -140,7 +169,7 @@ def test_struct_layouts_agree(tess, cname, pyname):
     header, the Python mirror and the Rust binding."""
     fields = c_struct_fields(cname)
     assert [f for f, _ in getattr(tess._capi, pyname)._fields_] == fields
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    text = open(RUST_FFI).read()
     body = re.search(r"pub struct " + cname + r" \{(.*?)\}", text, flags=re.S).group(1)
     assert re.findall(r"pub (\w+):", body) == fields
 

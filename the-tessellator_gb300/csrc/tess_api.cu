@@ -44,6 +44,33 @@ tess_status fail(tess_status st, const char* fmt, ...) {
         if (s_ != TESS_OK) return s_;                                                              \
     } while (0)
 
+// Timing events of one call (TESS_FLAG_TIMING), destroyed on every return
+// path, early error returns included.
+struct TimingEvents {
+    cudaEvent_t e[3] = {};
+    TimingEvents() = default;
+    TimingEvents(const TimingEvents&) = delete;
+    TimingEvents& operator=(const TimingEvents&) = delete;
+    ~TimingEvents() {
+        for (auto& x : e)
+            if (x) cudaEventDestroy(x);
+    }
+    cudaError_t create(int n) {
+        for (int i = 0; i < n; ++i) {
+            cudaError_t r = cudaEventCreate(&e[i]);
+            if (r != cudaSuccess) return r;
+        }
+        return cudaSuccess;
+    }
+    // elapsed milliseconds between two recorded events (0 when unavailable)
+    float ms(int a, int b) const {
+        float v = 0.f;
+        if (cudaEventElapsedTime(&v, e[a], e[b]) != cudaSuccess) v = 0.f;
+        (void)cudaGetLastError();   // best-effort timing leaves no error behind
+        return v;
+    }
+};
+
 template <typename T>
 tess_status dalloc(T** p, size_t count) {
     *p = nullptr;
@@ -375,16 +402,15 @@ GridBuffers grid_buffers(Engine& E) {
 
 tess_status engine_build(Engine& E, bool check) {
     CU(cudaSetDevice(E.device));
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TimingEvents ev;
     const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
     if (timing) {
-        CU(cudaEventCreate(&e0));
-        CU(cudaEventCreate(&e1));
-        CU(cudaEventRecord(e0, E.stream));
+        CU(ev.create(2));
+        CU(cudaEventRecord(ev.e[0], E.stream));
     }
     CU(launch_grid_build(grid_buffers(E), E.stream));
     E.launches += kGridLaunches;
-    if (timing) CU(cudaEventRecord(e1, E.stream));
+    if (timing) CU(cudaEventRecord(ev.e[1], E.stream));
     if (check) {
         int err = 0;
         CU(cudaMemcpyAsync(&err, E.d_err, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
@@ -393,13 +419,8 @@ tess_status engine_build(Engine& E, bool check) {
         if (err == 2) return fail(TESS_E_CUDA, "shell table exceeded its capacity");
     }
     if (timing) {
-        CU(cudaEventSynchronize(e1));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        (void)cudaGetLastError();   // best-effort timing leaves no error behind
-        E.stats.ms_grid = ms;
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        CU(cudaEventSynchronize(ev.e[1]));
+        E.stats.ms_grid = ev.ms(0, 1);
     }
     E.built = true;
     E.computed = false;
@@ -530,18 +551,10 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
     if (std::isnan(radius)) return fail(TESS_E_INVALID, "search_radius is NaN");
     CU(cudaSetDevice(E.device));
     const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
-    cudaEvent_t ev[3] = {};
-    struct EventGuard {
-        cudaEvent_t* e;
-        ~EventGuard() {
-            for (int i = 0; i < 3; ++i)
-                if (e[i]) cudaEventDestroy(e[i]);
-        }
-    } guard{ev};
-    if (timing)
-        for (auto& e : ev) CU(cudaEventCreate(&e));
+    TimingEvents ev;
+    if (timing) CU(ev.create(3));
     for (int attempt = 0; attempt < 4; ++attempt) {
-        TRY(enqueue_passes(E, precision, radius, group, timing, ev));
+        TRY(enqueue_passes(E, precision, radius, group, timing, ev.e));
         unsigned long long used = 0;
         unsigned counts[16];
         CU(cudaMemcpyAsync(&used, E.d_fcursor, sizeof(used), cudaMemcpyDeviceToHost, E.stream));
@@ -575,13 +588,8 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
             E.stats.table_entries = dd.tab_len;
         }
         if (timing) {
-            float a = 0, b = 0;
-            cudaEventElapsedTime(&a, ev[0], ev[1]);
-            cudaEventElapsedTime(&b, ev[1], ev[2]);
-            (void)cudaGetLastError();   // timing is best effort; leave no error behind
-            E.stats.ms_clip = a;
-            E.stats.ms_rerun = b;
-            // the events are destroyed by the guard at scope exit
+            E.stats.ms_clip = ev.ms(0, 1);
+            E.stats.ms_rerun = ev.ms(1, 2);
         }
         E.computed = true;
         E.csr_valid = false;
@@ -612,14 +620,11 @@ tess_status engine_csr(Engine& E) {
     if (!E.computed) return fail(TESS_E_STATE, "compute_all has not run");
     if (E.csr_valid) return TESS_OK;
     CU(cudaSetDevice(E.device));
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TimingEvents ev;
     const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
-    if (timing) {
-        CU(cudaEventCreate(&e0));
-        CU(cudaEventCreate(&e1));
-    }
+    if (timing) CU(ev.create(2));
     // offsets first (to size the outputs), then the gather
-    if (timing) CU(cudaEventRecord(e0, E.stream));
+    if (timing) CU(cudaEventRecord(ev.e[0], E.stream));
     CU(launch_csr_offsets(E.d_nface, E.total, E.d_offs, E.d_csr_tmp, E.stream));
     uint64_t total = 0;
     CU(cudaMemcpyAsync(&total, E.d_offs + E.total, sizeof(uint64_t), cudaMemcpyDeviceToHost, E.stream));
@@ -635,14 +640,9 @@ tess_status engine_csr(Engine& E) {
                          E.stream));
     E.launches += 4;
     if (timing) {
-        CU(cudaEventRecord(e1, E.stream));
-        CU(cudaEventSynchronize(e1));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        (void)cudaGetLastError();   // best-effort timing leaves no error behind
-        E.stats.ms_csr = ms;
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        CU(cudaEventRecord(ev.e[1], E.stream));
+        CU(cudaEventSynchronize(ev.e[1]));
+        E.stats.ms_csr = ev.ms(0, 1);
     }
     E.csr_total = total;
     E.csr_valid = true;
@@ -821,9 +821,9 @@ tess_status engine_radius(Engine& E, int mode, bool by_cell, const double* qxyz,
     const int blocks = (int)std::max<size_t>(1, std::min<size_t>((nq + 7) / 8, (size_t)E.sm_count * 16));
     CU(cudaMemsetAsync(E.d_rerr, 0, sizeof(int), E.stream));
     const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
-    cudaEvent_t ev[3] = {};
-    if (timing)
-        for (auto& e : ev) CU(cudaEventCreate(&e));
+    TimingEvents tev;
+    cudaEvent_t* ev = tev.e;
+    if (timing) CU(tev.create(3));
     E.stats.ms_query_count = E.stats.ms_query_fill = 0.0;
     uint64_t tot = 0;
     if (nq) {
@@ -860,12 +860,7 @@ tess_status engine_radius(Engine& E, int mode, bool by_cell, const double* qxyz,
     int err = 0;
     CU(cudaMemcpyAsync(&err, E.d_rerr, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
     CU(cudaStreamSynchronize(E.stream));
-    if (timing && nq) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ev[0], ev[1]);
-        (void)cudaGetLastError();   // best-effort timing leaves no error behind
-        E.stats.ms_query_count = ms;
-    }
+    if (timing && nq) E.stats.ms_query_count = tev.ms(0, 1);
     if (err) return fail(TESS_E_INVALID, "a query cell index is out of range (n = %u)", E.total);
     if (total) *total = (size_t)tot;
     if (offs) {
@@ -898,12 +893,7 @@ tess_status engine_radius(Engine& E, int mode, bool by_cell, const double* qxyz,
     E.launches += 1;
     if (!on_device) CU(cudaMemcpyAsync(out, E.d_rout, sizeof(uint32_t) * tot, cudaMemcpyDeviceToHost, E.stream));
     CU(cudaStreamSynchronize(E.stream));
-    if (timing) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ev[1], ev[2]);
-        (void)cudaGetLastError();   // best-effort timing leaves no error behind
-        E.stats.ms_query_fill = ms;
-    }
+    if (timing) E.stats.ms_query_fill = tev.ms(1, 2);
     return TESS_OK;
 }
 
@@ -1345,29 +1335,28 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
         if (ce != cudaSuccess) return fail(TESS_E_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
         E.graph_precision = prec;
     }
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TimingEvents ev;
     const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
     if (timing) {
-        CU(cudaEventCreate(&e0));
-        CU(cudaEventCreate(&e1));
-        CU(cudaEventRecord(e0, E.stream));
+        CU(ev.create(2));
+        CU(cudaEventRecord(ev.e[0], E.stream));
     }
     CU(cudaGraphLaunch(E.graph, E.stream));
     E.launches += kGridLaunches + (prec != TESS_PRECISION_FP64 ? 7 : 3);
-    if (timing) CU(cudaEventRecord(e1, E.stream));
+    if (timing) CU(cudaEventRecord(ev.e[1], E.stream));
     unsigned long long used = 0;
     unsigned counts[16];
+    int gerr = 0;
     CU(cudaMemcpyAsync(&used, E.d_fcursor, sizeof(used), cudaMemcpyDeviceToHost, E.stream));
     CU(cudaMemcpyAsync(counts, E.d_counters + 16, sizeof(counts), cudaMemcpyDeviceToHost, E.stream));
+    CU(cudaMemcpyAsync(&gerr, E.d_err, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
     CU(cudaStreamSynchronize(E.stream));
-    if (timing) {
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        (void)cudaGetLastError();   // best-effort timing leaves no error behind
-        E.stats.ms_clip = ms;
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+    if (timing) E.stats.ms_clip = ev.ms(0, 1);
+    if (gerr == 1) {
+        E.computed = false;
+        return fail(TESS_E_INVALID, "input coordinates must be finite");
     }
+    if (gerr == 2) return fail(TESS_E_CUDA, "shell table exceeded its capacity");
     if (used > E.face_cap) {
         // grow the pool; the captured graph holds the old pointer
         dfree(E.d_fnbr);
@@ -1394,6 +1383,18 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
     E.csr_valid = false;
     E.last_precision = prec;
     if (counts[L_FAIL]) return fail(TESS_E_OVERFLOW, "%u cells could not be computed", counts[L_FAIL]);
+    return TESS_OK;
+}
+
+tess_status tess_batch_update_points(tess_batch* b, const double* xyz, int on_device) {
+    if (!b || !xyz) return fail(TESS_E_INVALID, "NULL argument");
+    Engine& E = b->E;
+    CU(cudaSetDevice(E.device));
+    // the captured graph re-bins from d_xyz, so only the copy is enqueued here
+    CU(cudaMemcpyAsync(E.d_xyz, xyz, sizeof(double) * 3 * (size_t)E.total,
+                       on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, E.stream));
+    E.computed = false;
+    E.csr_valid = false;
     return TESS_OK;
 }
 

@@ -44,10 +44,11 @@
 // Crowded bins: a cell whose own bin holds many points is first cut by the
 // nearest point of each lane's stride of that bin (32 seeds, nearest first),
 // which shrinks it to about its final size before the shell walk.
+#pragma once
 #include <cfloat>
 #include <cmath>
+#include <mutex>
 
-#pragma once
 #include "tess_internal.cuh"
 
 namespace tess {
@@ -1719,14 +1720,24 @@ __global__ void __launch_bounds__(K == 2 ? 256 : 128, K == 2 ? 2 : 1) k_clip(Cli
     }
 }
 
-// Raise the kernel's dynamic shared memory limit to what `bytes` needs (once
-// per size); kept out of stream capture by the host's warm-up calls.
+// Raise the kernel's dynamic shared memory limit to what `bytes` needs, once
+// per size and device: cudaFuncSetAttribute applies to the current device
+// only, so the limit is remembered per device ordinal.  A mutex keeps two
+// host threads from lowering each other's limit.  Kept out of stream capture
+// by the host's warm-up calls.
+constexpr int kMaxDevices = 64;
 template <typename T, int K, bool GEO, int FORM>
 cudaError_t configure_smem(size_t bytes) {
-    static size_t configured = 0;
-    if (bytes <= configured) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_clip<T, K, GEO, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) configured = bytes;
+    static std::mutex mu;
+    static size_t configured[kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t* slot = (dev >= 0 && dev < kMaxDevices) ? &configured[dev] : nullptr;
+    if (slot && bytes <= *slot) return cudaSuccess;
+    e = cudaFuncSetAttribute(k_clip<T, K, GEO, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess && slot) *slot = bytes;
     return e;
 }
 

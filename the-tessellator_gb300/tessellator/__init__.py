@@ -435,6 +435,17 @@ class Batch:
         check(lib().tess_batch_compute(self._h, _prec(precision)))
         return self
 
+    def update_points(self, points=None, device_ptr: Optional[int] = None):
+        """Replace every diagram's points (same offsets and boxes); the next
+        compute() bins them again."""
+        if device_ptr is not None:
+            check(lib().tess_batch_update_points(self._h, C.c_void_p(device_ptr), 1))
+        else:
+            pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+            if len(pts) != self.n:
+                raise ValueError("update_points keeps the point count")
+            check(lib().tess_batch_update_points(self._h, C.c_void_p(pts.ctypes.data), 0))
+
     def volumes(self) -> np.ndarray:
         out = np.empty(self.n, dtype=np.float64)
         check(lib().tess_batch_volumes(self._h, _dp(out)))
