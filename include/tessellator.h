@@ -56,8 +56,9 @@ typedef enum {
     /* The FP32 + guard clipping (its exact topology and re-runs) with an
      * FP64-accurate finish: every vertex is refined by two Newton steps on its
      * three FP64 face planes, and face areas and volumes are accumulated in
-     * FP64 from those vertices.  Results meet the FP64 form's accuracy
-     * (volumes within 1e-12 relative) at close to the FP32 form's speed.
+     * FP64 from those vertices.  Volumes are within 1e-11 relative of the
+     * FP64 form (the worst of 1,000,000 uniform cells: 1.8e-12; typically
+     * 1e-14), at close to the FP32 form's speed.
      * Single-cell geometry queries run it as TESS_PRECISION_FP64. */
     TESS_PRECISION_MIXED = 2
 } tess_precision;
@@ -66,6 +67,13 @@ typedef enum {
 #define TESS_FLAG_TIMING 1u     /* record per-pass device times (tess_stats)          */
 #define TESS_FLAG_COUNTERS 2u   /* count the clipping work (tess_stats); the FP32 first pass then runs
                                    in its counting form, with the window pre-test (about 2% slower) */
+/* Flags that exercise the recovery paths (tests and diagnostics; results are
+ * unchanged except as stated): */
+#define TESS_FLAG_SMALL_FACE_POOL 4u  /* start the face pool at 1,024 faces, so a compute
+                                         overflows it and grows it (tess_stats.face_pool_regrows) */
+#define TESS_FLAG_NO_CAPACITY_RERUN 8u /* skip the larger-capacity re-runs: a cell that outgrows
+                                          the first pass's vertex or face slots is reported as
+                                          failed (TESS_E_OVERFLOW, volume 0, no faces) */
 
 typedef struct {
     /* FP32 form, guard band: a plane test of vertex v against the bisector of
@@ -127,6 +135,9 @@ typedef struct {
      * the first pass and computed by a pass that first cuts by the nearest
      * point of each lane's stride of that bin */
     uint64_t dense_cells;
+    /* times the face pool was found too small and grown, followed by a
+     * recompute, since the handle was created */
+    uint64_t face_pool_regrows;
 } tess_stats;
 
 void tess_config_default(tess_config* cfg);
@@ -319,6 +330,11 @@ tess_status tess_batch_volumes(tess_batch* b, double* volumes);
  * to each diagram. */
 tess_status tess_batch_neighbors_csr(tess_batch* b, uint64_t* offs, int32_t* nbr, double* area,
                                      size_t cap, size_t* total);
+/* Device pointers to the same results (valid until the next compute, update
+ * or destroy): volumes[total points], offs[total points + 1], nbr[faces],
+ * area[faces]; the batch form of tess_results_device. */
+tess_status tess_batch_results_device(tess_batch* b, const double** volumes, const uint64_t** offs,
+                                      const int32_t** nbr, const double** area, size_t* total);
 tess_status tess_batch_destroy(tess_batch* b);
 
 /* ------------------------------------------------------------------------ */

@@ -28,14 +28,14 @@ def _gather_rows(offs, vals, rows):
     return new, np.asarray(vals)[idx]
 
 
-def compare_sample(gpu, sample, ref):
+def compare_sample(gpu, sample, ref, all_mismatched=False):
     """Compare the GPU's results for the cells `sample` with the oracle's.
 
     gpu    = (volumes[n], offsets[n+1], neighbours, areas) of the whole diagram;
     sample = cell indices (original order) the oracle computed;
     ref    = (volumes, offsets, ids, areas) of the oracle for those cells.
     Returns a dict; 'mismatched_cells' lists up to 10 cells whose neighbour
-    lists differ."""
+    lists differ ('mismatched_all', with all_mismatched, every one of them)."""
     gv, go, gn, ga = gpu
     rv, ro, ri, ra = ref
     sample = np.asarray(sample, dtype=np.int64)
@@ -70,7 +70,8 @@ def compare_sample(gpu, sample, ref):
             if ok.any():
                 area_err = float(np.max(np.abs(ga2[ok] - ra2[ok]) / np.maximum(scale[ok], 1e-300)))
     bad = sample[~ident]
-    return {
+    extra = {"mismatched_all": bad} if all_mismatched else {}
+    return {**extra,
         "cells": int(len(sample)),
         "max_rel_vol_err": float(rel.max()) if len(rel) else 0.0,
         "mean_rel_vol_err": float(rel.mean()) if len(rel) else 0.0,
@@ -81,9 +82,11 @@ def compare_sample(gpu, sample, ref):
     }
 
 
-def symmetry_violations(offs, nbr, n, device=None):
-    """Number of (i, j) with j in N(i), j >= 0, and i not in N(j).  Runs on a
-    CUDA device through torch when one is given (large diagrams), else numpy."""
+def symmetry_violations(offs, nbr, n, device=None, areas=None, rel_area=None):
+    """Number of (i, j) with j in N(i), j >= 0, and i not in N(j).  With
+    `areas` and `rel_area`, only faces of at least rel_area of their cell's
+    largest face count (near-degenerate inputs).  Runs on a CUDA device
+    through torch when one is given (large diagrams), else numpy."""
     offs = np.asarray(offs, dtype=np.int64)
     counts = np.diff(offs)
     if device is not None:
@@ -93,9 +96,13 @@ def symmetry_violations(offs, nbr, n, device=None):
         rows = torch.repeat_interleave(torch.arange(n, device=device, dtype=torch.int64), o)
         cols = torch.from_numpy(np.ascontiguousarray(nbr)).to(device).to(torch.int64)
         keep = cols >= 0
-        rows, cols = rows[keep], cols[keep]
-        key, _ = torch.sort(rows * n + cols)
-        rkey = cols * n + rows
+        if areas is not None and rel_area is not None:
+            ar = torch.from_numpy(np.ascontiguousarray(areas)).to(device)
+            big = torch.zeros(n, dtype=ar.dtype, device=device).scatter_reduce_(0, rows, ar, "amax")
+            keep &= ar >= rel_area * big[rows]
+        rows_k, cols_k = rows[keep], cols[keep]
+        key, _ = torch.sort(rows[cols >= 0] * n + cols[cols >= 0])
+        rkey = cols_k * n + rows_k
         pos = torch.searchsorted(key, rkey).clamp_(max=max(int(key.numel()) - 1, 0))
         found = key[pos] == rkey if key.numel() else torch.zeros_like(rkey, dtype=torch.bool)
         res = int((~found).sum().item())
@@ -104,26 +111,42 @@ def symmetry_violations(offs, nbr, n, device=None):
     rows = np.repeat(np.arange(n, dtype=np.int64), counts)
     cols = np.asarray(nbr, dtype=np.int64)
     keep = cols >= 0
-    rows, cols = rows[keep], cols[keep]
-    key = np.sort(rows * n + cols)
-    rkey = cols * n + rows
+    if areas is not None and rel_area is not None:
+        ar = np.asarray(areas)
+        big = np.zeros(n)
+        np.maximum.at(big, rows, ar)
+        keep &= ar >= rel_area * big[rows]
+    key = np.sort(rows[cols >= 0] * n + cols[cols >= 0])
+    rkey = cols[keep] * n + rows[keep]
     if key.size == 0:
-        return 0
+        return int(rkey.size)
     pos = np.minimum(np.searchsorted(key, rkey), key.size - 1)
     return int(np.count_nonzero(key[pos] != rkey))
 
 
-def diagram_checks(vol, offs, nbr, box_volume, device=None):
+SLIVER_AREA = 1e-9
+
+
+def diagram_checks(vol, offs, nbr, box_volume, device=None, areas=None, rel_area=None):
     """Whole-diagram invariants: the volume sum against the box and the
-    neighbour symmetry."""
+    neighbour symmetry, counted strictly and, when areas are given, once more
+    with faces below rel_area (default SLIVER_AREA) of their cell's largest
+    face exempt: among tens of millions of random cells a few near-degenerate
+    vertex clusters leave slivers whose presence FP64 rounding decides, on
+    each side independently."""
     vol = np.asarray(vol)
     s = float(np.sum(vol, dtype=np.float64))
-    return {
+    out = {
         "vol_sum_minus_box": s - box_volume,
         "vol_sum_rel_err": abs(s - box_volume) / box_volume,
         "symmetry_violations": symmetry_violations(offs, nbr, len(vol), device),
         "faces": int(len(nbr)),
     }
+    if areas is not None:
+        ra = SLIVER_AREA if rel_area is None else rel_area
+        out["symmetry_violations_above_sliver"] = symmetry_violations(offs, nbr, len(vol), device, areas, ra)
+        out["sliver_area_rel"] = ra
+    return out
 
 
 def near_degenerate_ok(gpu_row, ref_row, rel_area=1e-9):
@@ -145,29 +168,26 @@ def near_degenerate_ok(gpu_row, ref_row, rel_area=1e-9):
     return worst <= rel_area, worst
 
 
-def near_degenerate_report(gpu, ref, rel_area=1e-9):
-    """Apply near_degenerate_ok to every cell of two whole-diagram results
-    (volumes, offsets, ids, areas).  Returns (cells with identical lists,
-    cells that differ only in tiny faces, cells that violate the criterion
-    (up to 10), the largest relative area of a differing face)."""
+def near_degenerate_report(gpu, ref, cells, rel_area=1e-9):
+    """Apply near_degenerate_ok to the given cells of two whole-diagram
+    results (volumes, offsets, ids, areas), typically the cells whose lists
+    differ.  Returns (cells that differ only in tiny faces, cells that violate
+    the criterion (up to 10), the largest relative area of a differing face)."""
     _, go, gn, ga = gpu
     _, ro, ri, ra = ref
     go = np.asarray(go, dtype=np.int64)
     ro = np.asarray(ro, dtype=np.int64)
-    n = len(go) - 1
-    same = tiny = 0
+    tiny = 0
     bad = []
     worst = 0.0
-    for i in range(n):
+    for i in cells:
+        i = int(i)
         g = (gn[go[i]:go[i + 1]], ga[go[i]:go[i + 1]])
         r = (ri[ro[i]:ro[i + 1]], ra[ro[i]:ro[i + 1]])
-        if len(g[0]) == len(r[0]) and np.array_equal(np.asarray(g[0], dtype=np.int64), np.asarray(r[0], dtype=np.int64)):
-            same += 1
-            continue
         ok, w = near_degenerate_ok(g, r, rel_area)
         worst = max(worst, w)
         if ok:
             tiny += 1
         elif len(bad) < 10:
             bad.append(i)
-    return same, tiny, bad, worst
+    return tiny, bad, worst

@@ -21,6 +21,8 @@ pub const TESS_PRECISION_FP32_GUARD: c_int = 1;
 pub const TESS_PRECISION_MIXED: c_int = 2;   // FP32 clipping, FP64-accurate results
 pub const TESS_FLAG_TIMING: u32 = 1;
 pub const TESS_FLAG_COUNTERS: u32 = 2;
+pub const TESS_FLAG_SMALL_FACE_POOL: u32 = 4;
+pub const TESS_FLAG_NO_CAPACITY_RERUN: u32 = 8;
 
 #[repr(C)] #[derive(Clone, Copy)]
 pub struct tess_config {
@@ -35,7 +37,7 @@ pub struct tess_stats {
     pub table_entries: u64, pub ms_grid: f64, pub ms_clip: f64, pub ms_rerun: f64, pub ms_csr: f64,
     pub launches: u64, pub rerun_guard: u64, pub rerun_verify: u64, pub rerun_degenerate: u64,
     pub candidates_tested: u64, pub cuts: u64, pub new_vertices: u64, pub windows: u64, pub batches: u64,
-    pub ms_query_count: f64, pub ms_query_fill: f64, pub rerun_fp64_full: u64, pub dense_cells: u64,
+    pub ms_query_count: f64, pub ms_query_fill: f64, pub rerun_fp64_full: u64, pub dense_cells: u64, pub face_pool_regrows: u64,
 }
 
 #[repr(C)]
@@ -110,6 +112,8 @@ extern "C" {
     pub fn tess_batch_volumes(b: *mut tess_batch, volumes: *mut f64) -> tess_status;
     pub fn tess_batch_neighbors_csr(b: *mut tess_batch, offs: *mut u64, nbr: *mut i32, area: *mut f64,
                                     cap: usize, total: *mut usize) -> tess_status;
+    pub fn tess_batch_results_device(b: *mut tess_batch, volumes: *mut *const f64, offs: *mut *const u64,
+                                     nbr: *mut *const i32, area: *mut *const f64, total: *mut usize) -> tess_status;
     pub fn tess_batch_destroy(b: *mut tess_batch) -> tess_status;
     // CSR offsets from device face counts, allocating nothing
     pub fn tess_csr_offsets_noalloc(d_counts: *const u32, n: usize, d_offs: *mut u64,

@@ -1,0 +1,184 @@
+"""GPU parity at the benchmarked sizes, through the C ABI, against the FP64
+oracle (all host threads).
+
+  * 16,777,216 uniform points (the headline workload): 200,000 evenly spaced
+    cells against the oracle; the whole diagram's volume sum and symmetry.
+  * 1,000,000 uniform points: every cell against the oracle, in the three
+    precisions.
+  * 4,194,304 clustered points: 20,000 evenly spaced cells; whole-diagram
+    invariants.
+  * 4,096 diagrams of 64 .. 65,536 points in one batch: 24 whole diagrams
+    (evenly spaced, plus the smallest and the largest) against per-diagram
+    oracles; every diagram's volume sum against its box; symmetry.
+  * The jittered lattices at full size (simple cubic 128^3, BCC 2 x 100^3):
+    every cell; the neighbour lists may differ from the oracle's only in
+    faces below 1e-9 of the cell's largest face (faces of area ~1e-14 whose
+    presence depends on the cut order at 1e-7 jitter), all else identical.
+
+Bars: neighbour lists bit-exact (general position); volumes within 1e-6
+(FP32 + guard), 1e-12 (FP64) or 1e-11 (mixed) relative; face areas within
+1e-5 or 1e-9 of the cell's largest face; volume sums within 1e-6 or 1e-11 of
+the box; neighbour relations symmetric except for slivers below 1e-9 of a
+cell's largest face (a few per ten million faces of random input, whose
+presence FP64 rounding decides on each side).
+"""
+import numpy as np
+import pytest
+
+from oracle import report
+
+pytestmark = pytest.mark.gpu
+
+# MIXED (FP32 clipping, two FP64-residual Newton steps per vertex): within
+# 1e-11; its worst cell of 1,000,000 uniform cells is at 1.8e-12
+VOL_TOL = {"fp64": 1e-12, "mixed": 1e-11, "fp32": 1e-6}
+AREA_TOL = {"fp64": 1e-9, "mixed": 1e-9, "fp32": 1e-5}
+SUM_TOL = {"fp64": 1e-11, "mixed": 1e-11, "fp32": 1e-6}
+DEGENERATE_AREA = 1e-9
+
+
+def gpu_run(T, pts, prec, lo=(0, 0, 0), hi=(1, 1, 1)):
+    with T.Diagram(pts, container=T.Polyhedron(*lo, *hi)) as d:
+        d.compute_all(prec)
+        vol = d.volumes()
+        offs, nbr, area = d.neighbors_csr()
+        st = d.stats()
+    return (vol, offs.astype(np.int64), nbr, area), st
+
+
+def check_sample(prec, gpu, sample, ref, box_volume=1.0):
+    c = report.compare_sample(gpu, sample, ref)
+    assert c["identical_neighbour_lists_pct"] == 100.0, c
+    assert c["max_rel_vol_err"] <= VOL_TOL[prec], c
+    assert c["max_area_err_rel_largest_face"] <= AREA_TOL[prec], c
+    d = report.diagram_checks(gpu[0], gpu[1], gpu[2], box_volume, "cuda", areas=gpu[3])
+    assert d["vol_sum_rel_err"] <= SUM_TOL[prec], d
+    # symmetric, but for slivers below 1e-9 of a cell's largest face (a few
+    # per ten million faces: near-degenerate vertex clusters of random input)
+    assert d["symmetry_violations_above_sliver"] == 0, d
+    assert d["symmetry_violations"] <= 1e-6 * d["faces"], d
+    print(f"{prec}: {c['cells']} cells compared, max rel vol err {c['max_rel_vol_err']:.2e}; "
+          f"asymmetric sliver faces {d['symmetry_violations']} of {d['faces']}")
+    return c, d
+
+
+def test_uniform_16m_sampled(tess, oracle_mod):
+    from tessellator import workloads
+
+    pts = workloads.uniform(16_777_216, seed=2)
+    sample = np.linspace(0, len(pts) - 1, 200_000).astype(np.uint32)
+    r = oracle_mod.Diagram(pts, lo=[0, 0, 0], hi=[1, 1, 1])
+    v, o, i, a, _, _ = r.compute_all(subset=sample)
+    del r
+    gpu, st = gpu_run(tess, pts, "fp32")
+    assert st["failed"] == 0
+    check_sample("fp32", gpu, sample, (v, o, i, a))
+
+
+@pytest.fixture(scope="module")
+def uniform1m(oracle_mod):
+    from tessellator import workloads
+
+    pts = workloads.uniform(1_000_000, seed=1)
+    r = oracle_mod.Diagram(pts, lo=[0, 0, 0], hi=[1, 1, 1])
+    v, o, i, a, _, _ = r.compute_all()
+    return pts, (v, o, i, a)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
+def test_uniform_1m_every_cell(tess, uniform1m, prec):
+    pts, ref = uniform1m
+    gpu, st = gpu_run(tess, pts, prec)
+    assert st["failed"] == 0
+    check_sample(prec, gpu, np.arange(len(pts)), ref)
+    if prec != "fp64":
+        assert st["rerun_fp64"] < 0.01 * len(pts)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
+def test_clustered_4m_sampled(tess, oracle_mod, prec):
+    from tessellator import workloads
+
+    pts = workloads.clustered(4_194_304, seed=3)
+    sample = np.linspace(0, len(pts) - 1, 20_000).astype(np.uint32)
+    r = oracle_mod.Diagram(pts, lo=[0, 0, 0], hi=[1, 1, 1])
+    v, o, i, a, _, _ = r.compute_all(subset=sample)
+    del r
+    gpu, st = gpu_run(tess, pts, prec)
+    assert st["failed"] == 0
+    check_sample(prec, gpu, sample, (v, o, i, a))
+    if prec != "fp64":
+        assert st["dense_cells"] > 0.1 * len(pts)      # the crowded-bin pass runs
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed"])
+def test_batch_4096_diagrams(tess, oracle_mod, prec):
+    import torch
+
+    from tessellator import workloads
+
+    pts, offs, boxes = workloads.batched(4096, seed=4)
+    offs64 = offs.astype(np.int64)
+    sizes = np.diff(offs64)
+    nd = len(sizes)
+    b = tess.Batch(pts, offs, boxes)
+    try:
+        b.compute(prec)
+        st = b.stats()
+        assert st["failed"] == 0
+        vp, op, np_, ap, total = b.results_device()
+        n = len(pts)
+        vol = torch.as_tensor(tess.DeviceArray(vp, n, np.float64), device="cuda")
+        go = torch.as_tensor(tess.DeviceArray(op, n + 1, np.uint64), device="cuda").to(torch.int64)
+        gn = torch.as_tensor(tess.DeviceArray(np_, total, np.int32), device="cuda")
+        ga = torch.as_tensor(tess.DeviceArray(ap, total, np.float64), device="cuda")
+        # every diagram's volumes add up to its box
+        bvol = np.prod(boxes[:, 3:] - boxes[:, :3], axis=1)
+        ids = torch.repeat_interleave(torch.arange(nd, device="cuda"), torch.as_tensor(sizes, device="cuda"))
+        dsum = torch.zeros(nd, dtype=torch.float64, device="cuda").index_add_(0, ids, vol).cpu().numpy()
+        assert np.max(np.abs(dsum - bvol) / bvol) <= SUM_TOL[prec]
+        # symmetry over the whole batch, with diagram-local ids made global
+        counts = (go[1:] - go[:-1])
+        base = torch.as_tensor(offs64[:-1], device="cuda")[ids]
+        gnb = torch.where(gn >= 0, gn.to(torch.int64) + torch.repeat_interleave(base, counts), -1)
+        asym = report.symmetry_violations(go.cpu().numpy(), gnb.cpu().numpy(), n, "cuda")
+        assert asym == 0
+        picks = set(np.linspace(0, nd - 1, 24).astype(np.int64).tolist())
+        picks |= {int(np.argmin(sizes)), int(np.argmax(sizes))}
+        go_h = go.cpu().numpy()
+        for d in sorted(picks):
+            a, e = int(offs64[d]), int(offs64[d + 1])
+            f0, f1 = int(go_h[a]), int(go_h[e])
+            sub = (vol[a:e].cpu().numpy(), go_h[a:e + 1] - f0, gn[f0:f1].cpu().numpy(), ga[f0:f1].cpu().numpy())
+            r = oracle_mod.Diagram(pts[a:e], lo=boxes[d, :3], hi=boxes[d, 3:])
+            rv, ro, ri, ra, _, _ = r.compute_all()
+            c = report.compare_sample(sub, np.arange(e - a), (rv, ro, ri, ra))
+            assert c["identical_neighbour_lists_pct"] == 100.0, (d, c)
+            assert c["max_rel_vol_err"] <= VOL_TOL[prec], (d, c)
+            assert c["max_area_err_rel_largest_face"] <= AREA_TOL[prec], (d, c)
+    finally:
+        b.close()
+
+
+@pytest.mark.parametrize("lattice,prec", [("sc", "fp32"), ("sc", "fp64"), ("bcc", "fp32"), ("bcc", "fp64")])
+def test_lattices_full_size(tess, oracle_mod, lattice, prec):
+    from tessellator import workloads
+
+    pts = workloads.lattice_sc(128, seed=5) if lattice == "sc" else workloads.lattice_bcc(100, seed=6)
+    r = oracle_mod.Diagram(pts, lo=[0, 0, 0], hi=[1, 1, 1])
+    ref = r.compute_all()[:4]
+    del r
+    gpu, st = gpu_run(tess, pts, prec)
+    assert st["failed"] == 0
+    c = report.compare_sample(gpu, np.arange(len(pts)), ref, all_mismatched=True)
+    # (FP64: 1e-9, not 1e-12: which near-degenerate slivers a cell keeps
+    # depends on the cut order, and moves its volume by ~1e-11)
+    assert c["max_rel_vol_err"] <= (1e-9 if prec == "fp64" else VOL_TOL["fp32"]), c
+    # the lists differ only in faces below DEGENERATE_AREA of the largest face
+    tiny, bad, worst = report.near_degenerate_report(gpu, ref, c["mismatched_all"], DEGENERATE_AREA)
+    assert not bad, (bad, worst)
+    assert tiny == c["mismatched_count"]
+    d = report.diagram_checks(gpu[0], gpu[1], gpu[2], 1.0, "cuda", areas=gpu[3], rel_area=DEGENERATE_AREA)
+    assert d["vol_sum_rel_err"] <= SUM_TOL["fp32"] and d["symmetry_violations"] == 0, d
+    print(f"{lattice} {prec}: {c['mismatched_count']} of {len(pts)} cells differ only in faces below "
+          f"{worst:.1e} of the largest; max rel vol err {c['max_rel_vol_err']:.1e}")

@@ -33,6 +33,28 @@ def compare(prec, gpu, ref, n, check_sum=None):
         assert abs(vol.sum() - check_sum) <= (1e-6 if prec == "fp32" else 1e-11) * check_sum
 
 
+def assert_only_tiny_faces_differ(gpu, ref, rel_area=1e-9):
+    """Near-degenerate inputs: the neighbour lists may differ only in faces
+    below rel_area of the cell's largest face (their presence depends on the
+    cut order); every other neighbour is identical."""
+    from oracle import report
+
+    c = report.compare_sample(gpu, np.arange(len(gpu[0])), ref, all_mismatched=True)
+    tiny, bad, worst = report.near_degenerate_report(gpu, ref, c["mismatched_all"], rel_area)
+    assert not bad, f"cells {bad} differ in faces up to {worst:.2e} of their largest face"
+    assert tiny == c["mismatched_count"]
+
+
+def canonical_lists(offs, nbr, rep):
+    """Each cell's neighbour set with ids mapped through rep (walls kept)."""
+    offs = np.asarray(offs, dtype=np.int64)
+    out = []
+    for i in range(len(offs) - 1):
+        ids = np.asarray(nbr[offs[i]:offs[i + 1]], dtype=np.int64)
+        out.append(sorted(set(np.where(ids >= 0, rep[np.maximum(ids, 0)], ids).tolist())))
+    return out
+
+
 def gpu_all(T, pts, prec, container=None, config=None, **kw):
     with T.Diagram(pts, container=container, config=config) as d:
         d.compute_all(prec, **kw)
@@ -217,10 +239,9 @@ def test_fp32_guard_reruns_on_lattice(tess, oracle_mod):
     assert np.max(np.abs(vol - rv) / rv) <= 1e-6
     assert abs(vol.sum() - 1.0) < 1e-6
     # 1e-7 jitter leaves faces of area ~1e-14 whose presence depends on the
-    # cut order (the FP64 form differs from the oracle the same way); the
-    # rest of each neighbour list must match
-    same = sum(np.array_equal(nbr[offs[i]:offs[i + 1]], ri[ro[i]:ro[i + 1]]) for i in range(len(pts)))
-    assert same >= 0.95 * len(pts)
+    # cut order (the FP64 form differs from the oracle the same way): the
+    # lists may differ only in faces below 1e-9 of the cell's largest face
+    assert_only_tiny_faces_differ((vol, offs.astype(np.int64), nbr, area), (rv, ro, ri, ra))
 
 
 def test_hybrid_rerun_on_bcc_lattice(tess, oracle_mod):
@@ -238,8 +259,7 @@ def test_hybrid_rerun_on_bcc_lattice(tess, oracle_mod):
     rv, ro, ri, ra = ref_all(oracle_mod, pts, [0, 0, 0], [1, 1, 1])
     assert np.max(np.abs(vol - rv) / rv) <= 1e-6
     assert abs(vol.sum() - 1.0) < 1e-6
-    same = sum(np.array_equal(nbr[offs[i]:offs[i + 1]], ri[ro[i]:ro[i + 1]]) for i in range(len(pts)))
-    assert same >= 0.99 * len(pts)
+    assert_only_tiny_faces_differ((vol, offs.astype(np.int64), nbr, area), (rv, ro, ri, ra))
 
 
 def test_clustered_small(tess, oracle_mod):
@@ -273,8 +293,9 @@ def test_near_duplicates_fp32(tess, oracle_mod):
     """Pairs 1e-12 .. 1e-5 apart and exact duplicates: the FP32 form hands the
     cells of pairs nearer than ~1e-6 to the FP64 form (bit-identical results
     there).  Cells bordering a pair meet two bisectors ~d apart, an
-    ill-conditioned sliver: elsewhere the bars are relaxed to 1e-9 (FP64 vs
-    the oracle) and 99% identical neighbour lists."""
+    ill-conditioned sliver: volumes are held to 1e-9 there (FP64 against the
+    oracle), and a pair that FP64 cannot separate counts as one site when the
+    neighbour lists are compared."""
     rng = np.random.default_rng(16)
     pts = rng.random((2000, 3))
     k = 0
@@ -286,8 +307,8 @@ def test_near_duplicates_fp32(tess, oracle_mod):
     g32, st = gpu_all(tess, pts, "fp32", container=unit_box(tess))
     g64, _ = gpu_all(tess, pts, "fp64", container=unit_box(tess))
     assert st["rerun_fp64"] >= 32 and st["failed"] == 0
-    v32, o32, n32, _ = g32
-    v64, o64, n64, _ = g64
+    v32, o32, n32, a32 = g32
+    v64, o64, n64, a64 = g64
     o32, o64 = o32.astype(np.int64), o64.astype(np.int64)
 
     def lists(o, nb, i):
@@ -296,7 +317,14 @@ def test_near_duplicates_fp32(tess, oracle_mod):
     for i in range(32):                 # pairs 0 .. 1e-7 apart: computed in FP64
         assert v32[i] == v64[i] and lists(o32, n32, i) == lists(o64, n64, i)
     np.testing.assert_allclose(v32, v64, rtol=1e-6)
-    assert sum(lists(o32, n32, i) == lists(o64, n64, i) for i in range(len(pts))) >= 0.99 * len(pts)
-    rv, ro, ri, _ = ref_all(oracle_mod, pts, [0, 0, 0], [1, 1, 1])
+    # A cell bordering a pair nearer than FP64 can separate (0, 1e-12, 1e-9,
+    # and 1e-7 apart) meets two nearly identical bisectors; which member of
+    # the pair takes the face and which the sliver (or nothing) is decided by
+    # rounding.  With each such pair counted as one site, every list is
+    # identical; the pairs 1e-5 apart are resolved and stay separate.
+    rep = np.arange(len(pts))
+    rep[1:32:2] = np.arange(0, 32, 2)
+    assert canonical_lists(o32, n32, rep) == canonical_lists(o64, n64, rep)
+    rv, ro, ri, ra = ref_all(oracle_mod, pts, [0, 0, 0], [1, 1, 1])
     np.testing.assert_allclose(v64, rv, rtol=1e-9)
-    assert sum(lists(o64, n64, i) == ri[ro[i]:ro[i + 1]].tolist() for i in range(len(pts))) >= 0.99 * len(pts)
+    assert canonical_lists(o64, n64, rep) == canonical_lists(ro, ri, rep)

@@ -356,7 +356,7 @@ tess_status engine_init(Engine& E, const tess_config* cfg, std::vector<DiagDesc>
     TRY(dalloc(&E.d_nface, n));
     TRY(dalloc(&E.d_fstart, n));
     TRY(dalloc(&E.d_status, n));
-    E.face_cap = (uint64_t)n * 20 + 4096;
+    E.face_cap = (E.cfg.flags & TESS_FLAG_SMALL_FACE_POOL) ? 1024 : (uint64_t)n * 20 + 4096;
     TRY(dalloc(&E.d_fnbr, E.face_cap));
     TRY(dalloc(&E.d_farea, E.face_cap));
     TRY(dalloc(&E.d_fcursor, 1));
@@ -415,8 +415,15 @@ tess_status engine_build(Engine& E, bool check) {
         int err = 0;
         CU(cudaMemcpyAsync(&err, E.d_err, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
         CU(cudaStreamSynchronize(E.stream));
-        if (err == 1) return fail(TESS_E_INVALID, "input coordinates must be finite");
-        if (err == 2) return fail(TESS_E_CUDA, "shell table exceeded its capacity");
+        if (err) {
+            // the grid describes the bad points: nothing may use it until a
+            // build succeeds
+            E.built = false;
+            E.computed = false;
+            E.csr_valid = false;
+            if (err == 1) return fail(TESS_E_INVALID, "input coordinates must be finite");
+            return fail(TESS_E_CUDA, "shell table exceeded its capacity");
+        }
     }
     if (timing) {
         CU(cudaEventSynchronize(ev.e[1]));
@@ -456,6 +463,7 @@ ClipParams base_params(Engine& E) {
     p.face_cap = E.face_cap;
     p.guard_rel = (float)E.cfg.guard_rel;
     p.verify_rel = (float)E.cfg.verify_rel;
+    p.grid_err = E.d_err;
     return p;
 }
 
@@ -498,6 +506,9 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
     };
     uint32_t* const* L = E.d_list;
     if (timing) CU(cudaEventRecord(ev[0], E.stream));
+    // without capacity re-runs, the capacity lists are left out: an overflowing
+    // cell is then reported as failed
+    const bool norerun = E.cfg.flags & TESS_FLAG_NO_CAPACITY_RERUN;
     if (precision == TESS_PRECISION_FP32_GUARD || precision == TESS_PRECISION_MIXED) {
         // with the exact flag (MIXED) every FP32 pass finishes in FP64
         const int X = precision == TESS_PRECISION_MIXED ? kFormExact : 0;
@@ -506,15 +517,15 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         // capacity re-runs at 4 and 8 slots; the flagged cells re-run in the
         // hybrid form (guard-band tests decided in FP64); what that cannot
         // settle runs in the FP64 form.
-        const bool two = s0 < 4, one = s0 < 8;
+        const bool two = s0 < 4, one = s0 < 8 && !norerun;
         // (with TESS_FLAG_COUNTERS the first pass runs in the standard form:
         // the lean form keeps no counters)
         const bool lean = s0 <= 2 && !(E.cfg.flags & TESS_FLAG_COUNTERS);
         TRY(pass(1, s0, (lean ? kFormLean : kFormStd) | X, nullptr, nullptr, L[L_FP64], cnt + L_FP64,
                  one ? L[L_CAP1] : nullptr, cnt + L_CAP1, lean ? L[L_DENSE] : nullptr, cnt + L_DENSE));
         if (lean)
-            TRY(pass(1, 2, kFormStd | X, L[L_DENSE], cnt + L_DENSE, L[L_FP64], cnt + L_FP64, L[L_CAP1],
-                     cnt + L_CAP1));
+            TRY(pass(1, 2, kFormStd | X, L[L_DENSE], cnt + L_DENSE, L[L_FP64], cnt + L_FP64,
+                     norerun ? nullptr : L[L_CAP1], cnt + L_CAP1));
         if (timing) CU(cudaEventRecord(ev[1], E.stream));
         if (one) {
             const int s1 = two ? 4 : 8;
@@ -523,13 +534,14 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
             if (two)
                 TRY(pass(1, 8, kFormStd | X, L[L_CAP2], cnt + L_CAP2, L[L_FP64], cnt + L_FP64, nullptr, nullptr));
         }
-        TRY(pass(1, 2, kFormHybrid | X, L[L_FP64], cnt + L_FP64, L[L_FP64B], cnt + L_FP64B, L[L_FP64B],
-                 cnt + L_FP64B));
-        TRY(pass(0, 2, kFormStd, L[L_FP64B], cnt + L_FP64B, nullptr, nullptr, L[L_CAP64A], cnt + L_CAP64A));
+        TRY(pass(1, 2, kFormHybrid | X, L[L_FP64], cnt + L_FP64, L[L_FP64B], cnt + L_FP64B,
+                 norerun ? nullptr : L[L_FP64B], cnt + L_FP64B));
+        TRY(pass(0, 2, kFormStd, L[L_FP64B], cnt + L_FP64B, nullptr, nullptr, norerun ? nullptr : L[L_CAP64A],
+                 cnt + L_CAP64A));
         TRY(pass(0, 4, kFormStd, L[L_CAP64A], cnt + L_CAP64A, nullptr, nullptr, L[L_CAP64B], cnt + L_CAP64B));
         TRY(pass(0, 8, kFormStd, L[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
     } else {
-        const bool two = s0 < 4, one = s0 < 8;
+        const bool two = s0 < 4, one = s0 < 8 && !norerun;
         TRY(pass(0, s0, kFormStd, nullptr, nullptr, nullptr, nullptr, one ? L[L_CAP64A] : nullptr, cnt + L_CAP64A));
         if (timing) CU(cudaEventRecord(ev[1], E.stream));
         if (one) {
@@ -557,9 +569,17 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
         TRY(enqueue_passes(E, precision, radius, group, timing, ev.e));
         unsigned long long used = 0;
         unsigned counts[16];
+        int gerr = 0;
         CU(cudaMemcpyAsync(&used, E.d_fcursor, sizeof(used), cudaMemcpyDeviceToHost, E.stream));
         CU(cudaMemcpyAsync(counts, E.d_counters + 16, sizeof(counts), cudaMemcpyDeviceToHost, E.stream));
+        CU(cudaMemcpyAsync(&gerr, E.d_err, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
         CU(cudaStreamSynchronize(E.stream));
+        if (gerr == 1) {
+            // the device points were rebuilt without a check and hold a
+            // non-finite coordinate: the clipping kernels did nothing
+            E.computed = false;
+            return fail(TESS_E_INVALID, "input coordinates must be finite");
+        }
         if (used > E.face_cap) {
             // face pool too small: grow and recompute
             dfree(E.d_fnbr);
@@ -567,6 +587,7 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
             E.face_cap = std::max<uint64_t>(2 * E.face_cap, used + used / 4 + 4096);
             TRY(dalloc(&E.d_fnbr, E.face_cap));
             TRY(dalloc(&E.d_farea, E.face_cap));
+            E.stats.face_pool_regrows += 1;
             continue;
         }
         E.stats.cells = E.total;
@@ -1364,6 +1385,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
         E.face_cap = used + used / 4 + 4096;
         TRY(dalloc(&E.d_fnbr, E.face_cap));
         TRY(dalloc(&E.d_farea, E.face_cap));
+        E.stats.face_pool_regrows += 1;
         cudaGraphExecDestroy(E.graph);
         E.graph = nullptr;
         return tess_batch_compute(b, precision);
@@ -1418,6 +1440,18 @@ tess_status tess_batch_neighbors_csr(tess_batch* b, uint64_t* offs, int32_t* nbr
                                      size_t* total) {
     if (!b) return fail(TESS_E_INVALID, "batch is NULL");
     return csr_out(b->E, offs, nbr, area, cap, total);
+}
+
+tess_status tess_batch_results_device(tess_batch* b, const double** volumes, const uint64_t** offs,
+                                      const int32_t** nbr, const double** area, size_t* total) {
+    if (!b) return fail(TESS_E_INVALID, "batch is NULL");
+    TRY(engine_csr(b->E));
+    if (volumes) *volumes = b->E.d_vol;
+    if (offs) *offs = b->E.d_offs;
+    if (nbr) *nbr = b->E.d_cnbr;
+    if (area) *area = b->E.d_carea;
+    if (total) *total = b->E.csr_total;
+    return TESS_OK;
 }
 
 tess_status tess_batch_destroy(tess_batch* b) {

@@ -1701,6 +1701,7 @@ __global__ void __launch_bounds__(K == 2 ? 256 : 128, K == 2 ? 2 : 1) k_clip(Cli
     extern __shared__ __align__(16) unsigned char smraw[];
     Smem<T, K>& S = reinterpret_cast<Smem<T, K>*>(smraw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
+    if (P.grid_err && *P.grid_err == 1) return;   // non-finite input: nothing to clip
     Work W;
     for (;;) {
         unsigned w = 0;

@@ -264,6 +264,10 @@ struct ClipParams {
     double point[3];
     int box_override;             // 1: walls from box[] instead of the diagram's box
     double box[6];                // lo xyz, hi xyz
+    // the binning pass's error flag: when it reports non-finite input (1),
+    // the clipping kernels return at once (the batch graph runs every pass
+    // without a host check in between)
+    const int* grid_err;
 };
 
 // Forms of the clipping kernel:

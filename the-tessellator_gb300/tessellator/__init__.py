@@ -30,12 +30,13 @@ from typing import List, Optional
 
 import numpy as np
 
-from ._capi import (FLAG_COUNTERS, FLAG_TIMING, PRECISION_FP32_GUARD, PRECISION_FP64, PRECISION_MIXED,
+from ._capi import (FLAG_COUNTERS, FLAG_NO_CAPACITY_RERUN, FLAG_SMALL_FACE_POOL, FLAG_TIMING, PRECISION_FP32_GUARD,
+                    PRECISION_FP64, PRECISION_MIXED,
                     CellGeometry, Config, Stats, TessError, check, default_config, last_error, lib)
 
-__all__ = ["Polyhedron", "Diagram", "Cell", "VoronoiFace", "Batch", "TessError", "Config",
+__all__ = ["Polyhedron", "Diagram", "Cell", "VoronoiFace", "Batch", "DeviceArray", "TessError", "Config",
            "default_config", "PRECISION_FP64", "PRECISION_FP32_GUARD", "PRECISION_MIXED", "FLAG_TIMING",
-           "FLAG_COUNTERS", "lib",
+           "FLAG_COUNTERS", "FLAG_SMALL_FACE_POOL", "FLAG_NO_CAPACITY_RERUN", "lib",
            "last_error"]
 
 # "mixed": the FP32 + guard clipping with an FP64-accurate finish (FP64-grade
@@ -62,6 +63,20 @@ def _radius(r: Optional[float]) -> float:
 
 def _group(g: Optional[int]) -> int:
     return -1 if g is None else int(g)
+
+
+class DeviceArray:
+    """A device buffer of the library (results_device) exposed through the
+    CUDA array interface, so torch.as_tensor(DeviceArray(...), device="cuda")
+    (or any consumer of the interface) views it without a copy.  The buffer
+    stays owned by the library: it is valid until the next compute, update or
+    destroy of its handle."""
+
+    _TYPES = {np.float64: "<f8", np.uint64: "<u8", np.int32: "<i4", np.uint32: "<u4"}
+
+    def __init__(self, ptr: int, count: int, dtype):
+        self.__cuda_array_interface__ = {"shape": (int(count),), "typestr": self._TYPES[np.dtype(dtype).type],
+                                         "data": (int(ptr), False), "version": 3, "strides": None}
 
 
 class Polyhedron:
@@ -462,6 +477,14 @@ class Batch:
         check(L.tess_batch_neighbors_csr(self._h, None, nbr.ctypes.data_as(C.POINTER(C.c_int32)), _dp(area),
                                          len(nbr), C.byref(total)))
         return offs, nbr[:total.value], area[:total.value]
+
+    def results_device(self):
+        """Device addresses (volumes, offsets, neighbour ids, areas, total faces)."""
+        v, o, nb, a = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+        total = C.c_size_t(0)
+        check(lib().tess_batch_results_device(self._h, C.byref(v), C.byref(o), C.byref(nb), C.byref(a),
+                                              C.byref(total)))
+        return v.value, o.value, nb.value, a.value, total.value
 
     def stats(self) -> dict:
         s = Stats()

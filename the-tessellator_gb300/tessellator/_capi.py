@@ -18,6 +18,8 @@ STATUS_NAMES = {0: "TESS_OK", 1: "TESS_E_INVALID", 2: "TESS_E_CUDA", 3: "TESS_E_
 PRECISION_FP64, PRECISION_FP32_GUARD, PRECISION_MIXED = 0, 1, 2
 FLAG_TIMING = 1
 FLAG_COUNTERS = 2
+FLAG_SMALL_FACE_POOL = 4
+FLAG_NO_CAPACITY_RERUN = 8
 MAX_CELL_VERTICES, MAX_CELL_FACES = 255, 254
 
 # Every function the header declares, in header order.
@@ -32,7 +34,7 @@ EXPORTS = (
     "tess_find_cells_in_radius", "tess_find_neighbors_in_radius", "tess_neighbor_cloud",
     "tess_neighbor_cloud_at",
     "tess_batch_create", "tess_batch_compute", "tess_batch_update_points", "tess_batch_stats", "tess_batch_volumes",
-    "tess_batch_neighbors_csr", "tess_batch_destroy", "tess_csr_offsets_noalloc",
+    "tess_batch_neighbors_csr", "tess_batch_results_device", "tess_batch_destroy", "tess_csr_offsets_noalloc",
 )
 
 
@@ -52,7 +54,7 @@ class Stats(C.Structure):
                 ("candidates_tested", C.c_uint64), ("cuts", C.c_uint64), ("new_vertices", C.c_uint64),
                 ("windows", C.c_uint64), ("batches", C.c_uint64), ("ms_query_count", C.c_double),
                 ("ms_query_fill", C.c_double), ("rerun_fp64_full", C.c_uint64),
-                ("dense_cells", C.c_uint64)]
+                ("dense_cells", C.c_uint64), ("face_pool_regrows", C.c_uint64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -125,6 +127,7 @@ def lib():
         "tess_batch_stats": (st, [vp, C.POINTER(Stats)]),
         "tess_batch_volumes": (st, [vp, dp]),
         "tess_batch_neighbors_csr": (st, [vp, u64p, i32p, dp, C.c_size_t, szp]),
+        "tess_batch_results_device": (st, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), szp]),
         "tess_batch_destroy": (st, [vp]),
         "tess_csr_offsets_noalloc": (st, [vp, C.c_size_t, vp, vp]),
     }
