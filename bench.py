@@ -174,6 +174,43 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def _cpulist(text):
+    out = set()
+    for part in text.strip().split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            out.update(range(int(a), int(b) + 1))
+        elif part:
+            out.add(int(part))
+    return out
+
+
+def bind_to_gpu_node(local):
+    """Run on the CPUs of the GPU's NUMA node, so pinned host buffers are
+    allocated (first touch) next to the GPU's host link.  Returns a record
+    for the JSON line and the previous affinity (restored before the
+    CPU-only legs)."""
+    import torch
+
+    before = os.sched_getaffinity(0)
+    nodes = sorted(int(d[4:]) for d in os.listdir("/sys/devices/system/node") if d.startswith("node")) \
+        if os.path.isdir("/sys/devices/system/node") else []
+    rec = {"numa_nodes": len(nodes), "gpu_node": None, "bound_cpus": len(before)}
+    try:
+        pr = torch.cuda.get_device_properties(local)
+        bus = f"{pr.pci_domain_id:04x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0"
+        node = int(open(f"/sys/bus/pci/devices/{bus}/numa_node").read().strip())
+        rec["gpu_node"] = node
+        if node >= 0 and len(nodes) > 1:
+            cpus = _cpulist(open(f"/sys/devices/system/node/node{node}/cpulist").read()) & before
+            if cpus:
+                os.sched_setaffinity(0, cpus)
+                rec["bound_cpus"] = len(cpus)
+    except (OSError, ValueError, AttributeError):
+        pass
+    return rec, before
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -321,8 +358,9 @@ def run_ours(args, ws, rank, local):
     import tessellator as T
 
     torch.cuda.set_device(local)
+    numa, affinity = bind_to_gpu_node(local)
     dist = dist_init(ws, "nccl")
-    pts, batched = make_points(args.workload)
+    pts, batched = make_points(args.workload, args.points if args.workload.startswith("uniform") else None)
     n = len(pts)
     stream = torch.cuda.Stream()
     cfg = T.default_config(flags=T.FLAG_TIMING, stream=stream.cuda_stream, device=local)
@@ -452,6 +490,9 @@ def run_ours(args, ws, rank, local):
                    "verify": int(st1["rerun_verify"]), "degenerate": int(st1["rerun_degenerate"]),
                    "rerun_fraction": int(st1["rerun_fp64"]) / n},
     }
+    if e2e is not None:
+        e2e["host"] = numa
+    os.sched_setaffinity(0, affinity)          # the CPU baseline uses every host thread
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(pts, batched, args.cpu_seconds)
@@ -535,8 +576,10 @@ PREC_DESC = {"fp32": "FP32 + FP64 guard re-run", "fp64": "FP64",
 def config_of(workload, n, nbytes):
     """The workload, identical in both arms' lines (the arm-specific precision
     and step descriptions are top-level keys)."""
-    return {"workload": WORKLOADS[workload]["desc"], "cells": n, "parallelism": "replicas",
-            "l2": l2_note(nbytes, 12 * n * 15.5)}
+    desc = WORKLOADS[workload]["desc"]
+    if workload.startswith("uniform") and n != WORKLOADS[workload]["n"]:
+        desc = f"{n:,} points i.i.d. uniform in [0,1]^3 (seed {WORKLOADS[workload]['seed']})"
+    return {"workload": desc, "cells": n, "parallelism": "replicas", "l2": l2_note(nbytes, 12 * n * 15.5)}
 
 
 def precision_leg(obj, lp, args, stream, base, local):
@@ -893,7 +936,7 @@ def main():
     ap.add_argument("--no-legs", action="store_true",
                     help="headline only: skip the MIXED, FP64, clustered and batched legs")
     ap.add_argument("--points", type=int, default=None,
-                    help="uniform / radius workloads only: this many points instead (profiling runs)")
+                    help="uniform and radius workloads only: this many points instead (profiling runs)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":

@@ -74,6 +74,9 @@ typedef enum {
 #define TESS_FLAG_NO_CAPACITY_RERUN 8u /* skip the larger-capacity re-runs: a cell that outgrows
                                           the first pass's vertex or face slots is reported as
                                           failed (TESS_E_OVERFLOW, volume 0, no faces) */
+#define TESS_FLAG_AUTOTUNE 16u  /* the first compute of a handle autotunes its launch knobs
+                                   (tess_diagram_autotune / tess_batch_autotune with the default
+                                   cache file) before it runs */
 
 typedef struct {
     /* FP32 form, guard band: a plane test of vertex v against the bisector of
@@ -100,6 +103,10 @@ typedef struct {
     /* cudaStream_t to run on; NULL: the library's own stream. */
     void* stream;
     uint32_t flags;
+    /* A cell whose own bin holds at least this many points first cuts by the
+     * nearest point of each lane's stride of that bin (crowded bins); 0: 48.
+     * A launch knob only: results do not depend on it. */
+    int32_t crowded_bin;
 } tess_config;
 
 /* Work and timing figures of the last tess_diagram_compute_all. */
@@ -336,6 +343,44 @@ tess_status tess_batch_neighbors_csr(tess_batch* b, uint64_t* offs, int32_t* nbr
 tess_status tess_batch_results_device(tess_batch* b, const double** volumes, const uint64_t** offs,
                                       const int32_t** nbr, const double** area, size_t* total);
 tess_status tess_batch_destroy(tess_batch* b);
+
+/* ------------------------------------------------------------------------ */
+/* Autotuning (no reference counterpart; the reference fixes its bin density  */
+/* with "TODO: Experiment with different values", celery.rs:185-188)          */
+/* ------------------------------------------------------------------------ */
+/* The knobs a compute runs with, chosen per input by timing every candidate
+ * on an evenly spaced sample of the cells (bin order, so the sample covers
+ * the whole box and every diagram of a batch).  Results never depend on
+ * them: they change how the work is laid out, not what is computed. */
+typedef struct {
+    int32_t warps_per_block;   /* chosen warps per block of the clipping kernel      */
+    int32_t crowded_bin;       /* chosen crowded-bin threshold (tess_config)        */
+    double bin_density;        /* batch: chosen points per bin of the batch's grid;
+                                  diagram: the Celery grid's density, unchanged, as
+                                  the bin queries expose that grid                  */
+    double ms_chosen;          /* the sample's compute time with the chosen knobs   */
+    double ms_default;         /* ... with the default knobs                        */
+    uint64_t sample_cells;     /* cells in the timing sample                         */
+    int32_t trials;            /* candidate knob sets timed (0: read from the cache) */
+    int32_t from_cache;        /* 1: the choice came from the cache file             */
+    uint32_t max_bin_points;   /* the input's most crowded bin (points)             */
+    double crowded_fraction;   /* share of points in bins of >= 48 points           */
+} tess_tuning;
+
+/* Tune d's knobs for `precision`.  The choice is kept by the handle for every
+ * later compute and written to a cache file, keyed by the device, the form
+ * (diagram / batch), the precision, the point count (power-of-two bucket) and
+ * the bin occupancy (most crowded bin, crowded share), so the next handle of
+ * that kind of input reuses it without timing.  cache_path: the file; NULL:
+ * $TESS_TUNE_CACHE, else $XDG_CACHE_HOME/tessellator-gb300/tuning.txt, else
+ * $HOME/.cache/tessellator-gb300/tuning.txt; "" : no cache.  The timing runs
+ * leave no results: call tess_diagram_compute_all afterwards. */
+tess_status tess_diagram_autotune(tess_diagram* d, tess_precision precision, const char* cache_path,
+                                  tess_tuning* out);
+/* The same for a batch, whose grid density is tuned too (the batch exposes no
+ * bin queries); the batch's CUDA graph is captured again with the choice. */
+tess_status tess_batch_autotune(tess_batch* b, tess_precision precision, const char* cache_path,
+                                tess_tuning* out);
 
 /* ------------------------------------------------------------------------ */
 /* No-allocation CSR offsets                                                  */

@@ -23,12 +23,13 @@ pub const TESS_FLAG_TIMING: u32 = 1;
 pub const TESS_FLAG_COUNTERS: u32 = 2;
 pub const TESS_FLAG_SMALL_FACE_POOL: u32 = 4;
 pub const TESS_FLAG_NO_CAPACITY_RERUN: u32 = 8;
+pub const TESS_FLAG_AUTOTUNE: u32 = 16;
 
 #[repr(C)] #[derive(Clone, Copy)]
 pub struct tess_config {
     pub guard_rel: f64, pub verify_rel: f64, pub bin_density: f64,
     pub table_gaps: i32, pub warps_per_block: i32, pub slots_per_lane: i32, pub device: i32,
-    pub stream: *mut c_void, pub flags: u32,
+    pub stream: *mut c_void, pub flags: u32, pub crowded_bin: i32,
 }
 
 #[repr(C)] #[derive(Clone, Copy, Default)]
@@ -38,6 +39,13 @@ pub struct tess_stats {
     pub launches: u64, pub rerun_guard: u64, pub rerun_verify: u64, pub rerun_degenerate: u64,
     pub candidates_tested: u64, pub cuts: u64, pub new_vertices: u64, pub windows: u64, pub batches: u64,
     pub ms_query_count: f64, pub ms_query_fill: f64, pub rerun_fp64_full: u64, pub dense_cells: u64, pub face_pool_regrows: u64,
+}
+
+#[repr(C)] #[derive(Clone, Copy, Default, Debug)]
+pub struct tess_tuning {
+    pub warps_per_block: i32, pub crowded_bin: i32, pub bin_density: f64, pub ms_chosen: f64,
+    pub ms_default: f64, pub sample_cells: u64, pub trials: i32, pub from_cache: i32,
+    pub max_bin_points: u32, pub crowded_fraction: f64,
 }
 
 #[repr(C)]
@@ -115,6 +123,11 @@ extern "C" {
     pub fn tess_batch_results_device(b: *mut tess_batch, volumes: *mut *const f64, offs: *mut *const u64,
                                      nbr: *mut *const i32, area: *mut *const f64, total: *mut usize) -> tess_status;
     pub fn tess_batch_destroy(b: *mut tess_batch) -> tess_status;
+    // autotuning of the launch knobs (sample-timed, cached)
+    pub fn tess_diagram_autotune(d: *mut tess_diagram, precision: c_int, cache_path: *const c_char,
+                                 out: *mut tess_tuning) -> tess_status;
+    pub fn tess_batch_autotune(b: *mut tess_batch, precision: c_int, cache_path: *const c_char,
+                               out: *mut tess_tuning) -> tess_status;
     // CSR offsets from device face counts, allocating nothing
     pub fn tess_csr_offsets_noalloc(d_counts: *const u32, n: usize, d_offs: *mut u64,
                                     stream: *mut c_void) -> tess_status;

@@ -46,7 +46,8 @@ fn check(st: tess_status) -> Result<(), Error> {
 
 /// Arithmetic of the clipping: plain FP64 (the reference's type), FP32 with
 /// FP64 guard-band re-runs (volumes to about 1e-7), or FP32 clipping with an
-/// FP64-accurate finish (volumes to 1e-12).  Neighbour lists are the same.
+/// FP64-accurate finish (volumes within 1e-11 of FP64).  Neighbour lists are
+/// the same.
 #[derive(Clone, Copy, Debug, PartialEq)]
 pub enum Precision {
     Fp64,
@@ -151,6 +152,14 @@ impl Diagram {
         let mut area = vec![0.0f64; total];
         check(unsafe { tess_neighbors_csr(self.h, ptr::null_mut(), nbr.as_mut_ptr(), area.as_mut_ptr(), total, &mut total) })?;
         Ok((offs, nbr, area))
+    }
+
+    /// Pick the clipping launch knobs for these points (timed on a sample of
+    /// the cells, cached on disk); later computes use them.
+    pub fn autotune(&mut self, precision: Precision) -> Result<tess_tuning, Error> {
+        let mut t = tess_tuning::default();
+        check(unsafe { tess_diagram_autotune(self.h, precision.code(), ptr::null(), &mut t) })?;
+        Ok(t)
     }
 
     /// get_cell_at_index (interface.rs:186-208).
@@ -355,6 +364,13 @@ impl Batch {
 
     pub fn compute(&mut self, precision: Precision) -> Result<(), Error> {
         check(unsafe { tess_batch_compute(self.h, precision.code()) })
+    }
+
+    /// As Diagram::autotune, with the batch's grid density among the knobs.
+    pub fn autotune(&mut self, precision: Precision) -> Result<tess_tuning, Error> {
+        let mut t = tess_tuning::default();
+        check(unsafe { tess_batch_autotune(self.h, precision.code(), ptr::null(), &mut t) })?;
+        Ok(t)
     }
 
     /// New positions for every diagram (same sizes and boxes).

@@ -163,7 +163,8 @@ def c_struct_fields(name):
     return names
 
 
-@pytest.mark.parametrize("cname,pyname", [("tess_stats", "Stats"), ("tess_config", "Config")])
+@pytest.mark.parametrize("cname,pyname", [("tess_stats", "Stats"), ("tess_config", "Config"),
+                                           ("tess_tuning", "Tuning")])
 def test_struct_layouts_agree(tess, cname, pyname):
     """tess_stats and tess_config: the same fields in the same order in the
     header, the Python mirror and the Rust binding."""

@@ -6,10 +6,14 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
 #include <vector>
+
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include "tess_internal.cuh"
 #include "tessellator.h"
@@ -83,6 +87,17 @@ template <typename T>
 void dfree(T*& p) {
     if (p) cudaFree((void*)p);
     p = nullptr;
+}
+
+// Device buffer of at least `need` elements (contents not kept).
+template <typename T>
+tess_status ensure(T** p, size_t& cap, size_t need) {
+    if (*p && need <= cap) return TESS_OK;
+    dfree(*p);
+    const size_t c = std::max(need, cap + cap / 2);
+    TRY(dalloc(p, c));
+    cap = c;
+    return TESS_OK;
 }
 
 // cells_per_dimension = (n / density).cbrt() as usize + 1 (celery.rs:159-160),
@@ -208,6 +223,14 @@ struct Engine {
     cudaGraphExec_t graph = nullptr;
     int graph_precision = -1;
     int blocks_cache[2][4][8] = {};   // [kernel type][slots][form, with the exact flag]
+    // allocated capacities of the grid arrays a re-grid may grow
+    uint64_t delims_alloc = 0, table_alloc = 0;
+    // autotuning: the timing sample, the occupancy counters, and whether the
+    // knobs were tuned for this handle
+    uint32_t* d_sample = nullptr;
+    size_t sample_cap = 0;
+    unsigned long long* d_occ = nullptr;
+    bool tuned = false;
 
     ~Engine() { release(); }
 
@@ -224,6 +247,7 @@ struct Engine {
         dfree(d_geo); dfree(d_one);
         dfree(d_rq); dfree(d_rcell); dfree(d_rcnt); dfree(d_roffs); dfree(d_rtmp); dfree(d_rout); dfree(d_rtab);
         dfree(d_rerr); dfree(d_gtab); dfree(d_bnd); dfree(d_qbin); dfree(d_qrank); dfree(d_qorder); dfree(d_qcnt); dfree(d_qcoff); dfree(d_qtmp);
+        dfree(d_sample); dfree(d_occ);
         if (own_stream && stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -245,6 +269,8 @@ struct Engine {
     }
 };
 
+constexpr int32_t kDefaultCrowdedBin = 48;
+
 void fill_defaults(tess_config* c) {
     c->guard_rel = 4e-7;
     c->verify_rel = 1e-6;
@@ -255,6 +281,7 @@ void fill_defaults(tess_config* c) {
     c->device = 0;
     c->stream = nullptr;
     c->flags = 0;
+    c->crowded_bin = kDefaultCrowdedBin;
 }
 
 tess_status check_config(const tess_config& c) {
@@ -267,6 +294,37 @@ tess_status check_config(const tess_config& c) {
     if (!(c.guard_rel >= 3e-7) || !(c.guard_rel < 1e-2))
         return fail(TESS_E_INVALID, "guard_rel must be in [3e-7, 1e-2)");
     if (!(c.verify_rel > 0.0) || !(c.verify_rel < 1.0)) return fail(TESS_E_INVALID, "verify_rel must be in (0, 1)");
+    if (c.crowded_bin != 0 && (c.crowded_bin < 2 || c.crowded_bin > (1 << 20)))
+        return fail(TESS_E_INVALID, "crowded_bin must be 0 (default) or in [2, 2^20]");
+    return TESS_OK;
+}
+
+// Per diagram: cells per dimension at `density`, the first global bin, and
+// the shell table's capacity and offset (cpd and the table extent follow
+// CeleryCellInfo::new, celery.rs:153-188).  Returns the totals.
+tess_status layout_grid(std::vector<DiagDesc>& diags, double density, int table_gaps, uint64_t* bins_out,
+                        uint64_t* tab_out) {
+    uint64_t bins = 0, tab = 0;
+    for (size_t d = 0; d < diags.size(); ++d) {
+        DiagDesc& D = diags[d];
+        const int64_t cpd = cells_per_dim(D.n, density);
+        if (cpd > 1625) return fail(TESS_E_INVALID, "diagram %zu: %u points give %lld bins per axis (max 1625)",
+                                    d, D.n, (long long)cpd);
+        D.cpd = (int32_t)cpd;
+        D.bin_base = bins;
+        bins += (uint64_t)cpd * cpd * cpd;
+        int c = table_gaps + 1;
+        if (c > cpd - 1) c = (int)cpd - 1;
+        if (c < 0) c = 0;
+        const uint64_t cube = (uint64_t)(2 * c + 1) * (2 * c + 1) * (2 * c + 1);
+        D.tab_cap = (uint32_t)std::min<uint64_t>(cube, (uint64_t)kMaxTable);
+        D.tab_base = tab;
+        tab += D.tab_cap;
+        D.tab_len = 0;
+    }
+    if (bins + 1 >= 0xFFFFFFF0ull) return fail(TESS_E_INVALID, "too many bins (%llu)", (unsigned long long)bins);
+    *bins_out = bins;
+    *tab_out = tab;
     return TESS_OK;
 }
 
@@ -293,22 +351,9 @@ tess_status engine_init(Engine& E, const tess_config* cfg, std::vector<DiagDesc>
     E.ndiag = diags.size();
     uint64_t total = 0, bins = 0, tab = 0;
     std::vector<uint32_t> cdiag, cstart;
+    TRY(layout_grid(diags, E.cfg.bin_density, E.cfg.table_gaps, &bins, &tab));
     for (size_t d = 0; d < diags.size(); ++d) {
-        DiagDesc& D = diags[d];
-        const int64_t cpd = cells_per_dim(D.n, E.cfg.bin_density);
-        if (cpd > 1625) return fail(TESS_E_INVALID, "diagram %zu: %u points give %lld bins per axis (max 1625)",
-                                    d, D.n, (long long)cpd);
-        D.cpd = (int32_t)cpd;
-        D.bin_base = bins;
-        bins += (uint64_t)cpd * cpd * cpd;
-        int c = E.cfg.table_gaps + 1;
-        if (c > cpd - 1) c = (int)cpd - 1;
-        if (c < 0) c = 0;
-        const uint64_t cube = (uint64_t)(2 * c + 1) * (2 * c + 1) * (2 * c + 1);
-        D.tab_cap = (uint32_t)std::min<uint64_t>(cube, (uint64_t)kMaxTable);
-        D.tab_base = tab;
-        tab += D.tab_cap;
-        D.tab_len = 0;
+        const DiagDesc& D = diags[d];
         for (uint32_t s = 0; s < D.n; s += kChunk) {
             cdiag.push_back((uint32_t)d);
             cstart.push_back(D.pt_base + s);
@@ -316,7 +361,6 @@ tess_status engine_init(Engine& E, const tess_config* cfg, std::vector<DiagDesc>
         total += D.n;
     }
     if (total >= 0xFFFFFFF0ull) return fail(TESS_E_INVALID, "too many points (%llu)", (unsigned long long)total);
-    if (bins + 1 >= 0xFFFFFFF0ull) return fail(TESS_E_INVALID, "too many bins (%llu)", (unsigned long long)bins);
     E.total = (uint32_t)total;
     E.total_bins = bins;
     E.table_total = tab;
@@ -343,6 +387,7 @@ tess_status engine_init(Engine& E, const tess_config* cfg, std::vector<DiagDesc>
     TRY(dalloc(&E.d_rank, n));
     TRY(dalloc(&E.d_delims, E.total_bins + 1));
     TRY(dalloc(&E.d_scan_tmp, scan_tmp_words(E.total_bins + 1)));
+    E.delims_alloc = E.total_bins + 1;
     TRY(dalloc(&E.d_sorted, n));
     TRY(dalloc(&E.d_inv, n));
     TRY(dalloc(&E.d_spx, n));
@@ -351,6 +396,7 @@ tess_status engine_init(Engine& E, const tess_config* cfg, std::vector<DiagDesc>
     TRY(dalloc(&E.d_shi, 3 * n));
     TRY(dalloc(&E.d_slo, 3 * n));
     TRY(dalloc(&E.d_table, E.table_total));
+    E.table_alloc = E.table_total;
     TRY(dalloc(&E.d_err, 1));
     TRY(dalloc(&E.d_vol, n));
     TRY(dalloc(&E.d_nface, n));
@@ -464,6 +510,7 @@ ClipParams base_params(Engine& E) {
     p.guard_rel = (float)E.cfg.guard_rel;
     p.verify_rel = (float)E.cfg.verify_rel;
     p.grid_err = E.d_err;
+    p.seed_min = (uint32_t)(E.cfg.crowded_bin > 0 ? E.cfg.crowded_bin : kDefaultCrowdedBin);
     return p;
 }
 
@@ -471,7 +518,7 @@ ClipParams base_params(Engine& E) {
 // first pass, capacity re-runs, FP64 re-runs.  Counters: cursor c at
 // d_counters[c], list counts at d_counters[16 + list].
 tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t group, bool timing,
-                           cudaEvent_t* ev) {
+                           cudaEvent_t* ev, const uint32_t* sample = nullptr, uint32_t nsample = 0) {
     unsigned* cur = E.d_counters;
     unsigned* cnt = E.d_counters + 16;
     CU(cudaMemsetAsync(E.d_counters, 0, sizeof(unsigned) * 32, E.stream));
@@ -492,6 +539,7 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         p.list_dense_count = cdense;
         p.work = work;
         p.work_count = wcount;
+        if (work && !wcount) p.total = nsample;   // the first pass over a timing sample
         p.cursor = cur + cursor++;
         p.list_fp64 = l64;
         p.list_fp64_count = c64;
@@ -521,7 +569,7 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         // (with TESS_FLAG_COUNTERS the first pass runs in the standard form:
         // the lean form keeps no counters)
         const bool lean = s0 <= 2 && !(E.cfg.flags & TESS_FLAG_COUNTERS);
-        TRY(pass(1, s0, (lean ? kFormLean : kFormStd) | X, nullptr, nullptr, L[L_FP64], cnt + L_FP64,
+        TRY(pass(1, s0, (lean ? kFormLean : kFormStd) | X, sample, nullptr, L[L_FP64], cnt + L_FP64,
                  one ? L[L_CAP1] : nullptr, cnt + L_CAP1, lean ? L[L_DENSE] : nullptr, cnt + L_DENSE));
         if (lean)
             TRY(pass(1, 2, kFormStd | X, L[L_DENSE], cnt + L_DENSE, L[L_FP64], cnt + L_FP64,
@@ -542,7 +590,7 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
         TRY(pass(0, 8, kFormStd, L[L_CAP64B], cnt + L_CAP64B, nullptr, nullptr, nullptr, nullptr));
     } else {
         const bool two = s0 < 4, one = s0 < 8 && !norerun;
-        TRY(pass(0, s0, kFormStd, nullptr, nullptr, nullptr, nullptr, one ? L[L_CAP64A] : nullptr, cnt + L_CAP64A));
+        TRY(pass(0, s0, kFormStd, sample, nullptr, nullptr, nullptr, one ? L[L_CAP64A] : nullptr, cnt + L_CAP64A));
         if (timing) CU(cudaEventRecord(ev[1], E.stream));
         if (one) {
             const int s1 = two ? 4 : 8;
@@ -555,6 +603,8 @@ tess_status enqueue_passes(Engine& E, int precision, double radius, int64_t grou
     return TESS_OK;
 }
 
+tess_status engine_autotune(Engine& E, int precision, bool batch, const char* cache_path, tess_tuning* out);
+
 tess_status engine_compute(Engine& E, int precision, double radius, int64_t group) {
     if (!E.built) return fail(TESS_E_STATE, "diagram is not built");
     if (precision != TESS_PRECISION_FP64 && precision != TESS_PRECISION_FP32_GUARD &&
@@ -562,6 +612,7 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
         return fail(TESS_E_INVALID, "unknown precision %d", precision);
     if (std::isnan(radius)) return fail(TESS_E_INVALID, "search_radius is NaN");
     CU(cudaSetDevice(E.device));
+    if ((E.cfg.flags & TESS_FLAG_AUTOTUNE) && !E.tuned) TRY(engine_autotune(E, precision, false, nullptr, nullptr));
     const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
     TimingEvents ev;
     if (timing) CU(ev.create(3));
@@ -670,6 +721,253 @@ tess_status engine_csr(Engine& E) {
     return TESS_OK;
 }
 
+// ---- autotuning ----
+
+// Lay the grid out again at `density` (batch handles only: a diagram's grid is
+// the Celery the bin queries expose) and rebuild it.
+tess_status engine_regrid(Engine& E, double density) {
+    std::vector<DiagDesc> diags = E.hdesc;
+    uint64_t bins = 0, tab = 0;
+    TRY(layout_grid(diags, density, E.cfg.table_gaps, &bins, &tab));
+    CU(cudaSetDevice(E.device));
+    CU(cudaStreamSynchronize(E.stream));
+    if (bins + 1 > E.delims_alloc) {
+        dfree(E.d_delims);
+        dfree(E.d_scan_tmp);
+        TRY(dalloc(&E.d_delims, bins + 1));
+        TRY(dalloc(&E.d_scan_tmp, scan_tmp_words(bins + 1)));
+        E.delims_alloc = bins + 1;
+    }
+    if (tab > E.table_alloc) {
+        dfree(E.d_table);
+        TRY(dalloc(&E.d_table, tab));
+        E.table_alloc = tab;
+    }
+    E.hdesc = diags;
+    E.total_bins = bins;
+    E.table_total = tab;
+    E.cfg.bin_density = density;
+    CU(cudaMemcpyAsync(E.d_desc, E.hdesc.data(), sizeof(DiagDesc) * E.ndiag, cudaMemcpyHostToDevice, E.stream));
+    if (E.graph) cudaGraphExecDestroy(E.graph);
+    E.graph = nullptr;
+    return engine_build(E, true);
+}
+
+// The cache file of tuned knobs: explicit path, "" for none, else
+// $TESS_TUNE_CACHE, $XDG_CACHE_HOME/tessellator-gb300/tuning.txt or
+// $HOME/.cache/tessellator-gb300/tuning.txt.
+std::string tuning_cache_path(const char* given) {
+    if (given) return std::string(given);
+    if (const char* e = std::getenv("TESS_TUNE_CACHE")) return std::string(e);
+    std::string dir;
+    if (const char* x = std::getenv("XDG_CACHE_HOME")) dir = std::string(x) + "/tessellator-gb300";
+    else if (const char* h = std::getenv("HOME")) dir = std::string(h) + "/.cache/tessellator-gb300";
+    else return std::string();
+    return dir + "/tuning.txt";
+}
+
+// One line per key: "<key>\t<warps_per_block> <crowded_bin> <bin_density> <ms_chosen> <ms_default> <sample>".
+bool tuning_lookup(const std::string& path, const std::string& key, tess_tuning* t) {
+    if (path.empty()) return false;
+    FILE* f = std::fopen(path.c_str(), "r");
+    if (!f) return false;
+    char line[1024];
+    bool found = false;
+    while (std::fgets(line, sizeof(line), f)) {
+        const char* tab = std::strchr(line, '\t');
+        if (!tab || (size_t)(tab - line) != key.size() || std::strncmp(line, key.c_str(), key.size()) != 0) continue;
+        int w = 0, c = 0;
+        double d = 0, a = 0, b = 0;
+        unsigned long long m = 0;
+        if (std::sscanf(tab + 1, "%d %d %lf %lf %lf %llu", &w, &c, &d, &a, &b, &m) == 6 && w >= 1 && w <= 8 &&
+            c >= 2 && c <= (1 << 20) && d > 0.0 && std::isfinite(d)) {
+            t->warps_per_block = w;
+            t->crowded_bin = c;
+            t->bin_density = d;
+            t->ms_chosen = a;
+            t->ms_default = b;
+            t->sample_cells = m;
+            found = true;   // the last entry of a key wins
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+void tuning_store(const std::string& path, const std::string& key, const tess_tuning& t) {
+    if (path.empty()) return;
+    // create the directory (one level of parent is enough for the defaults)
+    const size_t slash = path.find_last_of('/');
+    if (slash != std::string::npos && slash > 0) {
+        const std::string dir = path.substr(0, slash);
+        const size_t up = dir.find_last_of('/');
+        if (up != std::string::npos && up > 0) mkdir(dir.substr(0, up).c_str(), 0755);
+        mkdir(dir.c_str(), 0755);
+    }
+    std::vector<std::string> keep;
+    if (FILE* f = std::fopen(path.c_str(), "r")) {
+        char line[1024];
+        while (std::fgets(line, sizeof(line), f)) {
+            const char* tab = std::strchr(line, '\t');
+            if (tab && (size_t)(tab - line) == key.size() && std::strncmp(line, key.c_str(), key.size()) == 0) continue;
+            keep.emplace_back(line);
+        }
+        std::fclose(f);
+    }
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s\t%d %d %.17g %.6f %.6f %llu\n", key.c_str(), t.warps_per_block, t.crowded_bin,
+                  t.bin_density, t.ms_chosen, t.ms_default, (unsigned long long)t.sample_cells);
+    keep.emplace_back(buf);
+    const std::string tmp = path + ".tmp" + std::to_string((long long)getpid());
+    FILE* f = std::fopen(tmp.c_str(), "w");
+    if (!f) return;
+    bool ok = true;
+    for (const auto& l : keep) ok &= std::fputs(l.c_str(), f) >= 0;
+    ok &= std::fclose(f) == 0;
+    if (ok) std::rename(tmp.c_str(), path.c_str());
+    else std::remove(tmp.c_str());
+}
+
+// Time one compute over the sample with the current knobs (ms), the face
+// pool grown first if the sample overflows it.
+tess_status time_sample(Engine& E, int precision, uint32_t m, float* ms) {
+    TimingEvents ev;
+    CU(ev.create(2));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        CU(cudaEventRecord(ev.e[0], E.stream));
+        TRY(enqueue_passes(E, precision, -1.0, -1, false, nullptr, E.d_sample, m));
+        CU(cudaEventRecord(ev.e[1], E.stream));
+        unsigned long long used = 0;
+        CU(cudaMemcpyAsync(&used, E.d_fcursor, sizeof(used), cudaMemcpyDeviceToHost, E.stream));
+        CU(cudaStreamSynchronize(E.stream));
+        if (used <= E.face_cap) {
+            *ms = ev.ms(0, 1);
+            return TESS_OK;
+        }
+        dfree(E.d_fnbr);
+        dfree(E.d_farea);
+        E.face_cap = std::max<uint64_t>(2 * E.face_cap, used + used / 4 + 4096);
+        TRY(dalloc(&E.d_fnbr, E.face_cap));
+        TRY(dalloc(&E.d_farea, E.face_cap));
+        E.stats.face_pool_regrows += 1;
+        if (E.graph) cudaGraphExecDestroy(E.graph);
+        E.graph = nullptr;
+    }
+    return fail(TESS_E_NOMEM, "face pool could not be sized");
+}
+
+// Choose warps per block, the crowded-bin threshold and (batches) the grid
+// density by timing each candidate on an evenly spaced sample of up to
+// 262,144 cells in bin order (the whole box, every diagram), two runs each,
+// the faster counted.  Candidates: warps per block {4, 8} (the clipping
+// kernel's launch bound allows 8 at most), crowded bin {32, 48, 96, 192},
+// density {0.6, 1.25, 2.5} points per bin (batches).
+tess_status engine_autotune(Engine& E, int precision, bool batch, const char* cache_path, tess_tuning* out) {
+    if (!E.built) return fail(TESS_E_STATE, "the grid is not built");
+    if (precision != TESS_PRECISION_FP64 && precision != TESS_PRECISION_FP32_GUARD && precision != TESS_PRECISION_MIXED)
+        return fail(TESS_E_INVALID, "unknown precision %d", precision);
+    CU(cudaSetDevice(E.device));
+    tess_tuning T{};
+    // the input's occupancy at the reference density
+    if (!E.d_occ) TRY(dalloc(&E.d_occ, 2));
+    const double dens0 = E.cfg.bin_density;
+    if (batch && dens0 != 1.25) TRY(engine_regrid(E, 1.25));
+    const int ob = (int)std::min<uint64_t>(4096, (E.total_bins + 255) / 256 + 1);
+    CU(launch_occupancy(E.d_delims, E.total_bins, (uint32_t)kDefaultCrowdedBin, E.d_occ, ob, E.stream));
+    unsigned long long occ[2] = {0, 0};
+    CU(cudaMemcpyAsync(occ, E.d_occ, sizeof(occ), cudaMemcpyDeviceToHost, E.stream));
+    CU(cudaStreamSynchronize(E.stream));
+    T.max_bin_points = (uint32_t)occ[0];
+    T.crowded_fraction = E.total ? (double)occ[1] / (double)E.total : 0.0;
+    cudaDeviceProp prop;
+    CU(cudaGetDeviceProperties(&prop, E.device));
+    char kb[512];
+    std::snprintf(kb, sizeof(kb), "%s/%dsm|%s|prec%d|n2^%d|max2^%d|crowd%d", prop.name, prop.multiProcessorCount,
+                  batch ? "batch" : "diagram", precision, (int)std::lround(std::log2((double)std::max(1u, E.total))),
+                  (int)std::floor(std::log2((double)occ[0] + 1.0)), (int)std::lround(10.0 * T.crowded_fraction));
+    std::string key(kb);
+    for (auto& ch : key)
+        if (ch == ' ' || ch == '\t' || ch == '\n') ch = '_';
+    const std::string path = tuning_cache_path(cache_path);
+    tess_tuning cached{};
+    if (tuning_lookup(path, key, &cached)) {
+        E.cfg.warps_per_block = cached.warps_per_block;
+        E.cfg.crowded_bin = cached.crowded_bin;
+        std::memset(E.blocks_cache, 0, sizeof(E.blocks_cache));
+        if (batch && cached.bin_density != E.cfg.bin_density) TRY(engine_regrid(E, cached.bin_density));
+        if (E.graph) cudaGraphExecDestroy(E.graph);
+        E.graph = nullptr;
+        cached.from_cache = 1;
+        cached.trials = 0;
+        cached.max_bin_points = T.max_bin_points;
+        cached.crowded_fraction = T.crowded_fraction;
+        if (!batch) cached.bin_density = E.cfg.bin_density;
+        E.tuned = true;
+        E.computed = false;
+        E.csr_valid = false;
+        if (out) *out = cached;
+        return TESS_OK;
+    }
+    // the sample: every k-th cell in bin (sorted) order
+    const uint32_t m = std::min<uint32_t>(E.total, 262144u);
+    std::vector<uint32_t> hs(m);
+    for (uint32_t i = 0; i < m; ++i) hs[i] = (uint32_t)(((uint64_t)i * E.total) / m);
+    TRY(ensure(&E.d_sample, E.sample_cap, m));
+    CU(cudaMemcpyAsync(E.d_sample, hs.data(), sizeof(uint32_t) * m, cudaMemcpyHostToDevice, E.stream));
+    T.sample_cells = m;
+    std::vector<double> dens = batch ? std::vector<double>{1.25, 0.6, 2.5} : std::vector<double>{E.cfg.bin_density};
+    const int wpbs[] = {8, 4};
+    const int crowds[] = {48, 32, 96, 192};
+    float best = INFINITY;
+    int bw = 8, bc = kDefaultCrowdedBin;
+    double bd = dens[0];
+    for (double de : dens) {
+        if (batch && de != E.cfg.bin_density) {
+            uint64_t nb = 0, nt = 0;
+            std::vector<DiagDesc> probe = E.hdesc;
+            if (layout_grid(probe, de, E.cfg.table_gaps, &nb, &nt) != TESS_OK) continue;   // too many bins
+            TRY(engine_regrid(E, de));
+        }
+        for (int w : wpbs)
+            for (int c : crowds) {
+                E.cfg.warps_per_block = w;
+                E.cfg.crowded_bin = c;
+                std::memset(E.blocks_cache, 0, sizeof(E.blocks_cache));
+                float t = INFINITY;
+                for (int rep = 0; rep < 2; ++rep) {
+                    float ms = 0.f;
+                    TRY(time_sample(E, precision, m, &ms));
+                    t = std::min(t, ms);
+                }
+                ++T.trials;
+                if (de == 1.25 && w == 8 && c == kDefaultCrowdedBin) T.ms_default = t;
+                if (t < best) {
+                    best = t;
+                    bw = w;
+                    bc = c;
+                    bd = de;
+                }
+            }
+    }
+    E.cfg.warps_per_block = bw;
+    E.cfg.crowded_bin = bc;
+    std::memset(E.blocks_cache, 0, sizeof(E.blocks_cache));
+    if (batch && bd != E.cfg.bin_density) TRY(engine_regrid(E, bd));
+    if (E.graph) cudaGraphExecDestroy(E.graph);
+    E.graph = nullptr;
+    T.warps_per_block = bw;
+    T.crowded_bin = bc;
+    T.bin_density = batch ? bd : E.cfg.bin_density;
+    T.ms_chosen = best;
+    if (!batch) T.ms_default = T.ms_default > 0 ? T.ms_default : best;
+    E.tuned = true;
+    E.computed = false;
+    E.csr_valid = false;
+    tuning_store(path, key, T);
+    if (out) *out = T;
+    return TESS_OK;
+}
+
 // One cell's full geometry: re-run the cell alone (FP64 re-run if the FP32
 // form declines it) into the GeoOut buffer and copy it back.
 tess_status engine_geo(Engine& E, int precision, uint32_t gs, const double* point, double radius, int64_t group,
@@ -708,16 +1006,6 @@ tess_status engine_geo(Engine& E, int precision, uint32_t gs, const double* poin
     return fail(TESS_E_OVERFLOW, "cell could not be computed (status %d)", out->status);
 }
 
-// Device buffer of at least `need` elements (contents not kept).
-template <typename T>
-tess_status ensure(T** p, size_t& cap, size_t need) {
-    if (*p && need <= cap) return TESS_OK;
-    dfree(*p);
-    const size_t c = std::max(need, cap + cap / 2);
-    TRY(dalloc(p, c));
-    cap = c;
-    return TESS_OK;
-}
 
 // Largest search-order prefix a neighbour-cloud call may enumerate.
 constexpr size_t kMaxRadiusTable = (size_t)1 << 26;
@@ -1331,6 +1619,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
     if (prec != TESS_PRECISION_FP64 && prec != TESS_PRECISION_FP32_GUARD && prec != TESS_PRECISION_MIXED)
         return fail(TESS_E_INVALID, "unknown precision %d", prec);
     CU(cudaSetDevice(E.device));
+    if ((E.cfg.flags & TESS_FLAG_AUTOTUNE) && !E.tuned) TRY(engine_autotune(E, prec, true, nullptr, nullptr));
     if (!E.graph || E.graph_precision != prec) {
         // warm the per-kernel attributes and occupancy queries outside capture
         for (int pr : {0, 1})
@@ -1452,6 +1741,17 @@ tess_status tess_batch_results_device(tess_batch* b, const double** volumes, con
     if (area) *area = b->E.d_carea;
     if (total) *total = b->E.csr_total;
     return TESS_OK;
+}
+
+tess_status tess_diagram_autotune(tess_diagram* d, tess_precision precision, const char* cache_path,
+                                  tess_tuning* out) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    return engine_autotune(d->E, (int)precision, false, cache_path, out);
+}
+
+tess_status tess_batch_autotune(tess_batch* b, tess_precision precision, const char* cache_path, tess_tuning* out) {
+    if (!b) return fail(TESS_E_INVALID, "batch is NULL");
+    return engine_autotune(b->E, (int)precision, true, cache_path, out);
 }
 
 tess_status tess_batch_destroy(tess_batch* b) {

@@ -68,12 +68,12 @@ constexpr bool kPrefetch = true;
 // first-pass form leaves it out: on uniform inputs windows are small and its
 // mere presence costs the hot loop registers.
 constexpr int kPretestMin = 2;
-// A site whose own bin holds at least this many points is seeded before the
-// shell walk: every lane takes the nearest point of its stride of that bin and
-// the 32 seeds are cut nearest first.  In crowded bins the walk's 32-point
-// windows otherwise meet the nearest points late, after many cuts by farther
-// ones (plane capacity, larger radius, more guard-band tests).
-constexpr unsigned kSeedMin = 48;
+// A site whose own bin holds at least ClipParams::seed_min points (48 by
+// default, autotuned per input) is seeded before the shell walk: every lane
+// takes the nearest point of its stride of that bin and the 32 seeds are cut
+// nearest first.  In crowded bins the walk's 32-point windows otherwise meet
+// the nearest points late, after many cuts by farther ones (plane capacity,
+// larger radius, more guard-band tests).
 // Hybrid form: a new FP32 vertex whose error bound exceeds kNumBad * guard_rel
 // * R (1e-3 R at the default guard_rel) sends the cell to the FP64 form.
 constexpr float kNumBad = 2500.0f;
@@ -1210,7 +1210,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     // skips the bins done here (27-bit mask `done` over the offsets {-1,0,1}^3).
     if constexpr (kSeedForm) {
         const uint64_t sb = bin_base + ((uint64_t)cbx * cpd + cby) * cpd + cbz;
-        if (P.delims[sb + 1] - P.delims[sb] >= kSeedMin) {
+        if (P.delims[sb + 1] - P.delims[sb] >= P.seed_min) {
             const int ti = lane / 9 - 1, tj = (lane / 3) % 3 - 1, tk = lane % 3 - 1;
             unsigned nbeg = 0, ncnt = 0;
             float nd = INFINITY;
@@ -1222,7 +1222,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 }
                 nd = lane == 13 ? 0.f : (near_ok ? near2(ti, tj, tk) : INFINITY);
             }
-            unsigned pending = __ballot_sync(FULL, ncnt >= kSeedMin && nd < INFINITY);
+            unsigned pending = __ballot_sync(FULL, ncnt >= P.seed_min && nd < INFINITY);
             const unsigned ndkey = (__float_as_uint(nd) & ~31u) | (unsigned)lane;
             while (pending && status == ST_OK) {
                 const unsigned best = __reduce_min_sync(FULL, ((pending >> lane) & 1u) ? ndkey : 0xFFFFFFFFu);
@@ -1265,7 +1265,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     if (kBatch2) load_entry(32 + lane, eb);
     // lean first pass: a crowded own bin (table entry 0, lane 0's first
     // entry) sends the cell to the seeded pass
-    if (BASE == kFormLean && P.list_dense && __shfl_sync(FULL, ea.cnt, 0) >= kSeedMin) status = ST_DENSE;
+    if (BASE == kFormLean && P.list_dense && __shfl_sync(FULL, ea.cnt, 0) >= P.seed_min) status = ST_DENSE;
     while (status == ST_OK) {
         // The table key is rounded toward zero and the threshold up, so
         // stopping on key >= thr never drops a bin that could hold a cutter.

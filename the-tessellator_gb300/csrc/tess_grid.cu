@@ -401,11 +401,37 @@ size_t scan_tmp_words(uint64_t nitems) {
 }
 
 namespace {
+// Bin occupancy for the autotuner: out[0] = most points in one bin, out[1] =
+// points in bins of at least `crowd` points.  One atomic per warp.
+__global__ void k_occupancy(const uint32_t* delims, uint64_t nbins, uint32_t crowd, unsigned long long* out) {
+    unsigned long long mx = 0, crowded = 0;
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = delims[b + 1] - delims[b];
+        mx = c > mx ? c : mx;
+        if (c >= crowd) crowded += c;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        crowded += __shfl_xor_sync(0xffffffffu, crowded, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&out[0], mx);
+        atomicAdd(&out[1], crowded);
+    }
+}
+
 __global__ void k_bounds_init(unsigned long long* b, int ndiag) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < 6 * ndiag) b[t] = (t % 6) < 3 ? ~0ull : 0ull;
 }
 }  // namespace
+
+cudaError_t launch_occupancy(const uint32_t* delims, uint64_t nbins, uint32_t crowd, unsigned long long* out,
+                             int blocks, cudaStream_t s) {
+    cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), s);
+    k_occupancy<<<blocks, 256, 0, s>>>(delims, nbins, crowd, out);
+    return cudaGetLastError();
+}
 
 // Binning pass: bounds -> grid parameters -> shell tables -> histogram ->
 // scan -> scatter -> within-bin order -> gather.  A fixed launch sequence

@@ -144,6 +144,10 @@ constexpr int kScanItems = 8;       // items per thread in the scan
 constexpr int kScanThreads = 1024;
 
 cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s);
+// out[0] = most points in one bin, out[1] = points in bins of >= crowd points
+// (every bin of every diagram of the set)
+cudaError_t launch_occupancy(const uint32_t* delims, uint64_t nbins, uint32_t crowd, unsigned long long* out,
+                             int blocks, cudaStream_t s);
 size_t scan_tmp_words(uint64_t nitems);
 
 // ---- radius queries (tess_radius.cu) ----
@@ -258,6 +262,7 @@ struct ClipParams {
     int64_t target_group;         // < 0: none
     float guard_rel;
     float verify_rel;
+    uint32_t seed_min;            // own-bin count from which a cell is seeded (crowded bins)
     // single-cell geometry output (queries); null for bulk runs
     GeoOut* geo;
     int at_point;                 // 1: site = point[] below, not a diagram point

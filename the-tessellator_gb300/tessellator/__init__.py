@@ -30,13 +30,13 @@ from typing import List, Optional
 
 import numpy as np
 
-from ._capi import (FLAG_COUNTERS, FLAG_NO_CAPACITY_RERUN, FLAG_SMALL_FACE_POOL, FLAG_TIMING, PRECISION_FP32_GUARD,
-                    PRECISION_FP64, PRECISION_MIXED,
-                    CellGeometry, Config, Stats, TessError, check, default_config, last_error, lib)
+from ._capi import (FLAG_AUTOTUNE, FLAG_COUNTERS, FLAG_NO_CAPACITY_RERUN, FLAG_SMALL_FACE_POOL, FLAG_TIMING,
+                    PRECISION_FP32_GUARD, PRECISION_FP64, PRECISION_MIXED,
+                    CellGeometry, Config, Stats, TessError, Tuning, check, default_config, last_error, lib)
 
 __all__ = ["Polyhedron", "Diagram", "Cell", "VoronoiFace", "Batch", "DeviceArray", "TessError", "Config",
            "default_config", "PRECISION_FP64", "PRECISION_FP32_GUARD", "PRECISION_MIXED", "FLAG_TIMING",
-           "FLAG_COUNTERS", "FLAG_SMALL_FACE_POOL", "FLAG_NO_CAPACITY_RERUN", "lib",
+           "FLAG_COUNTERS", "FLAG_SMALL_FACE_POOL", "FLAG_NO_CAPACITY_RERUN", "FLAG_AUTOTUNE", "lib",
            "last_error"]
 
 # "mixed": the FP32 + guard clipping with an FP64-accurate finish (FP64-grade
@@ -184,6 +184,15 @@ class Diagram:
         check(lib().tess_diagram_compute_all(self._h, _prec(precision), _radius(search_radius),
                                              _group(target_group)))
         return self
+
+    def autotune(self, precision="fp32", cache_path: Optional[str] = None) -> dict:
+        """Pick the clipping launch knobs for these points by timing candidates
+        on a sample of the cells (tess_diagram_autotune); later computes use
+        them.  cache_path None: the default cache file; "": no cache."""
+        t = Tuning()
+        cp = None if cache_path is None else cache_path.encode()
+        check(lib().tess_diagram_autotune(self._h, _prec(precision), cp, C.byref(t)))
+        return t.as_dict()
 
     def volumes(self) -> np.ndarray:
         out = np.empty(self.n, dtype=np.float64)
@@ -449,6 +458,13 @@ class Batch:
         Diagram.compute_all), in one CUDA-graph launch per precision."""
         check(lib().tess_batch_compute(self._h, _prec(precision)))
         return self
+
+    def autotune(self, precision="fp32", cache_path: Optional[str] = None) -> dict:
+        """As Diagram.autotune, with the batch's grid density among the knobs."""
+        t = Tuning()
+        cp = None if cache_path is None else cache_path.encode()
+        check(lib().tess_batch_autotune(self._h, _prec(precision), cp, C.byref(t)))
+        return t.as_dict()
 
     def update_points(self, points=None, device_ptr: Optional[int] = None):
         """Replace every diagram's points (same offsets and boxes); the next

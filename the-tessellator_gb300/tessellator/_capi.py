@@ -20,6 +20,7 @@ FLAG_TIMING = 1
 FLAG_COUNTERS = 2
 FLAG_SMALL_FACE_POOL = 4
 FLAG_NO_CAPACITY_RERUN = 8
+FLAG_AUTOTUNE = 16
 MAX_CELL_VERTICES, MAX_CELL_FACES = 255, 254
 
 # Every function the header declares, in header order.
@@ -34,7 +35,8 @@ EXPORTS = (
     "tess_find_cells_in_radius", "tess_find_neighbors_in_radius", "tess_neighbor_cloud",
     "tess_neighbor_cloud_at",
     "tess_batch_create", "tess_batch_compute", "tess_batch_update_points", "tess_batch_stats", "tess_batch_volumes",
-    "tess_batch_neighbors_csr", "tess_batch_results_device", "tess_batch_destroy", "tess_csr_offsets_noalloc",
+    "tess_batch_neighbors_csr", "tess_batch_results_device", "tess_batch_destroy",
+    "tess_diagram_autotune", "tess_batch_autotune", "tess_csr_offsets_noalloc",
 )
 
 
@@ -42,7 +44,7 @@ class Config(C.Structure):
     _fields_ = [("guard_rel", C.c_double), ("verify_rel", C.c_double), ("bin_density", C.c_double),
                 ("table_gaps", C.c_int32), ("warps_per_block", C.c_int32),
                 ("slots_per_lane", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("crowded_bin", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -55,6 +57,16 @@ class Stats(C.Structure):
                 ("windows", C.c_uint64), ("batches", C.c_uint64), ("ms_query_count", C.c_double),
                 ("ms_query_fill", C.c_double), ("rerun_fp64_full", C.c_uint64),
                 ("dense_cells", C.c_uint64), ("face_pool_regrows", C.c_uint64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("warps_per_block", C.c_int32), ("crowded_bin", C.c_int32), ("bin_density", C.c_double),
+                ("ms_chosen", C.c_double), ("ms_default", C.c_double), ("sample_cells", C.c_uint64),
+                ("trials", C.c_int32), ("from_cache", C.c_int32), ("max_bin_points", C.c_uint32),
+                ("crowded_fraction", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -129,6 +141,8 @@ def lib():
         "tess_batch_neighbors_csr": (st, [vp, u64p, i32p, dp, C.c_size_t, szp]),
         "tess_batch_results_device": (st, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), szp]),
         "tess_batch_destroy": (st, [vp]),
+        "tess_diagram_autotune": (st, [vp, C.c_int, C.c_char_p, C.POINTER(Tuning)]),
+        "tess_batch_autotune": (st, [vp, C.c_int, C.c_char_p, C.POINTER(Tuning)]),
         "tess_csr_offsets_noalloc": (st, [vp, C.c_size_t, vp, vp]),
     }
     for name in EXPORTS:
