@@ -57,6 +57,9 @@ NCU_CLIP_BYTES_PER_CELL = (74.728448e6 + 169.210368e6) / 1_000_000
 # kernel is bound by instruction issue, so this gives its issue roofline.
 NCU_CLIP_INST_PER_CELL = 13_133_793_392 / 1_000_000
 NCU_RADIUS_BYTES = {"count": 3.846207488e9 + 0.50285184e9, "fill": 6.337812736e9 + 1.53743616e9}
+# DRAM traffic of the 11 binning launches (read 706.5 MB + write 215.5 MB) at
+# 4,194,304 uniform points, scaled by points: every term is per point or per bin.
+NCU_GRID_BYTES_PER_POINT = (706.5e6 + 215.5e6) / 4_194_304
 
 
 def l2_note(input_bytes, written_bytes):
@@ -534,7 +537,10 @@ def run_ours(args, ws, rank, local):
             gach = gbytes / (np.mean(grid_ms) / 1e3) / 1e9
             out["roofline_grid"] = {"kernel": "binning pass (11 launches)", "bound": "hbm", "achieved": gach,
                                     "peak": hbm, "unit": "GB/s", "frac": gach / hbm,
-                                    "algorithmic_bytes": gbytes, "peak_source": src}
+                                    "algorithmic_bytes": gbytes, "peak_source": src,
+                                    "traffic": NCU_GRID_BYTES_PER_POINT * n,
+                                    "traffic_source": "ncu DRAM bytes of the 11 launches at 4,194,304 points, "
+                                                      "scaled by points"}
     if rank == 0 and gpu_res is not None:
         try:
             out["parity"] = dict(parity_report(gpu_res, base, 1.0, f"cuda:{local}"),

@@ -498,6 +498,7 @@ ClipParams base_params(Engine& E) {
     p.delims = E.d_delims;
     p.sgroup = E.d_sgroup;
     p.table = E.d_table;
+    p.bin = E.d_bin;
     p.total = E.total;
     p.vol = E.d_vol;
     p.nface = E.d_nface;

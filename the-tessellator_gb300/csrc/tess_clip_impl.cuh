@@ -110,10 +110,18 @@ struct Smem {
             uint16_t mapf[P], maps[P];
         };
         struct {                      // finalize
-            // FP32 form only: FP64 face planes {n, h} (n.x = h) and their
-            // distance from the site, and per-vertex FP32 corrections to the
-            // FP64 position
-            double qx[PF], qy[PF], qz[PF], qh[PF];
+            // FP32 forms only: face planes {n, h} (n.x = h), their distance
+            // from the site, and per-vertex FP32 corrections to the FP64
+            // position.  The FP64-accurate finish keeps the planes in FP64;
+            // the FP32 form keeps them as FP32 pairs: n = fq + ql, h = hh + hl.
+            union {
+                struct {
+                    double qx[PF], qy[PF], qz[PF], qh[PF];
+                };
+                struct {
+                    float qlx[PF], qly[PF], qlz[PF], qhh[PF], qhl[PF];
+                };
+            };
             float fqx[PF], fqy[PF], fqz[PF], qdist[PF];
             float dx[VF], dy[VF], dz[VF];
             double rx[VF], ry[VF], rz[VF];    // exact form: refined FP64 positions
@@ -189,6 +197,49 @@ __device__ __forceinline__ void set_k(uint32_t (&m)[K], int s) {
 }
 
 __device__ __forceinline__ int plane_of(uint32_t t, int i) { return (int)((t >> (8 * i)) & 0xFFu); }
+
+// Error-free transforms (Knuth's TwoSum; the product's rounding error by one
+// FMA): s + e == a + b and p + e == a * b exactly.  Explicit round-to-nearest
+// intrinsics keep the compiler from contracting or reordering them.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+    p = __fmul_rn(a, b);
+    e = __fmaf_rn(a, b, -p);
+}
+
+// q = b / d and r = b % d, exactly, for b < 2^32 and a quotient below 2^11
+// (bin coordinates: cpd <= 1625).  The FP32 estimate b * (1/d) carries three
+// roundings of 2^-24 relative, under 2e-4 on such a quotient, so its floor is
+// off by at most one and one correction step settles it.
+__device__ __forceinline__ void divmod_est(uint32_t b, uint32_t d, float rcp, uint32_t& q, uint32_t& r) {
+    long long qq = (long long)((float)b * rcp);
+    long long rr = (long long)b - qq * (long long)d;
+    if (rr < 0) {
+        --qq;
+        rr += d;
+    } else if (rr >= (long long)d) {
+        ++qq;
+        rr -= d;
+    }
+    q = (uint32_t)qq;
+    r = (uint32_t)rr;
+}
+
+// Bin coordinates of local bin id b = (x * cpd + y) * cpd + z
+// (get_cell_from_indices, celery.rs:317-325), without FP64.
+__device__ __forceinline__ void split_bin(uint32_t b, int cpd, float rcp, float rcp2, int& x, int& y, int& z) {
+    const uint32_t c = (uint32_t)cpd;
+    uint32_t qx, rx, qy, ry;
+    divmod_est(b, c * c, rcp2, qx, rx);
+    divmod_est(rx, c, rcp, qy, ry);
+    x = (int)qx;
+    y = (int)qy;
+    z = (int)ry;
+}
 
 // Signed distance n.v - offset.
 __device__ __forceinline__ float sdist(float nx, float ny, float nz, float off, float x, float y, float z) {
@@ -922,30 +973,49 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     }
     C.lm[0] = 0xFFu;
     C.np = 6;
+    // The FP32 first pass sets up without the FP64 pipe (dozens of cycles per
+    // warp instruction on this part): box offsets from the FP32 pairs of the
+    // box and the site relative to the centre, one rounding each side of the
+    // sum (<= 2^-23 relative) plus the pairs' own ~2^-47 of the extent.
+    constexpr bool kF32Setup = BASE == kFormLean;
     if (lane < 6) {
         const int a = lane >> 1;
         const bool mx = lane & 1;
-        const double s_a = a == 0 ? sx : (a == 1 ? sy : sz);
-        const double off = mx ? (bhi[a] - s_a) : (s_a - blo[a]);
+        T offt;
+        if constexpr (kF32Setup) {
+            const float sh_a = a == 0 ? shx : (a == 1 ? shy : shz);
+            const float sl_a = a == 0 ? slx : (a == 1 ? sly : slz);
+            offt = mx ? ((D.bhi_hi[a] - sh_a) + (D.bhi_lo[a] - sl_a)) : ((sh_a - D.blo_hi[a]) + (sl_a - D.blo_lo[a]));
+        } else {
+            const double s_a = a == 0 ? sx : (a == 1 ? sy : sz);
+            offt = (T)(mx ? (bhi[a] - s_a) : (s_a - blo[a]));
+        }
         const T sg = mx ? (T)1 : (T)-1;
         S.px[lane] = a == 0 ? sg : (T)0;
         S.py[lane] = a == 1 ? sg : (T)0;
         S.pz[lane] = a == 2 ? sg : (T)0;
-        S.pd[lane] = (T)off;
+        S.pd[lane] = offt;
         S.pn[lane] = (T)1;
         S.pid[lane] = -1 - lane;   // -1 x_min, -2 x_max, -3 y_min, -4 y_max, -5 z_min, -6 z_max
     }
     if (lane < 8) {
         const int bx = lane & 1, by = (lane >> 1) & 1, bz = (lane >> 2) & 1;
-        C.vx[0] = (T)((bx ? bhi[0] : blo[0]) - sx);
-        C.vy[0] = (T)((by ? bhi[1] : blo[1]) - sy);
-        C.vz[0] = (T)((bz ? bhi[2] : blo[2]) - sz);
+        if constexpr (kF32Setup) {
+            C.vx[0] = bx ? ((D.bhi_hi[0] - shx) + (D.bhi_lo[0] - slx)) : ((D.blo_hi[0] - shx) + (D.blo_lo[0] - slx));
+            C.vy[0] = by ? ((D.bhi_hi[1] - shy) + (D.bhi_lo[1] - sly)) : ((D.blo_hi[1] - shy) + (D.blo_lo[1] - sly));
+            C.vz[0] = bz ? ((D.bhi_hi[2] - shz) + (D.bhi_lo[2] - slz)) : ((D.blo_hi[2] - shz) + (D.blo_lo[2] - slz));
+        } else {
+            C.vx[0] = (T)((bx ? bhi[0] : blo[0]) - sx);
+            C.vy[0] = (T)((by ? bhi[1] : blo[1]) - sy);
+            C.vz[0] = (T)((bz ? bhi[2] : blo[2]) - sz);
+        }
         S.vx[lane] = C.vx[0];
         S.vy[lane] = C.vy[0];
         S.vz[lane] = C.vz[0];
         if constexpr (GUARD) {
-            // rounding of the FP64 box corner to FP32
-            C.ve[0] = ((T)1.2e-7 + (T)P.guard_rel) * (fabs(C.vx[0]) + fabs(C.vy[0]) + fabs(C.vz[0]));
+            // the corner's rounding to FP32: 2^-24 relative per component from
+            // FP64, 2^-23 from the FP32 pairs (doubled here)
+            C.ve[0] = ((T)(kF32Setup ? 2.5e-7 : 1.2e-7) + (T)P.guard_rel) * (fabs(C.vx[0]) + fabs(C.vy[0]) + fabs(C.vz[0]));
             S.ve[lane] = C.ve[0];
         }
         const int pX = bx, pY = 2 + by, pZ = 4 + bz;
@@ -989,9 +1059,15 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
 
     // ---- the walk over bins in shell order (celery.rs:1023-1075) ----
     const int cpd = D.cpd;
-    const int cbx = axis_index(sx, D.glo[0], D.ghi[0], D.inv[0], cpd);
-    const int cby = axis_index(sy, D.glo[1], D.ghi[1], D.inv[1], cpd);
-    const int cbz = axis_index(sz, D.glo[2], D.ghi[2], D.inv[2], cpd);
+    int cbx, cby, cbz;
+    if constexpr (kF32Setup) {
+        // the site's bin from the binning pass (bit-exact axis_index there)
+        split_bin(P.bin[orig] - (uint32_t)bin_base, cpd, D.rcp_cpd, D.rcp_cpd2, cbx, cby, cbz);
+    } else {
+        cbx = axis_index(sx, D.glo[0], D.ghi[0], D.inv[0], cpd);
+        cby = axis_index(sy, D.glo[1], D.ghi[1], D.inv[1], cpd);
+        cbz = axis_index(sz, D.glo[2], D.ghi[2], D.inv[2], cpd);
+    }
     const double radius = P.search_radius;
     const bool has_radius = radius >= 0.0;
     const int64_t tgroup = P.target_group;
@@ -1141,20 +1217,30 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     // test than the gap key: a point of bin (b + o) lies at least
     // |o| - 1 + f (o < 0) or o - f (o > 0) bin sides from the site on each
     // axis.  Off-grid sites (cells of external points) skip the test.
-    const float fx = (float)(__dmul_rn(sx - D.glo[0], D.inv[0]) - (double)cbx);
-    const float fy = (float)(__dmul_rn(sy - D.glo[1], D.inv[1]) - (double)cby);
-    const float fz = (float)(__dmul_rn(sz - D.glo[2], D.inv[2]) - (double)cbz);
+    float fx, fy, fz;
+    if constexpr (kF32Setup) {
+        // (x - glo) * inv from the FP32 pairs: within D.frac_eps bins
+        fx = ((shx - D.glo_hi[0]) + (slx - D.glo_lo[0])) * D.inv_f[0] - (float)cbx;
+        fy = ((shy - D.glo_hi[1]) + (sly - D.glo_lo[1])) * D.inv_f[1] - (float)cby;
+        fz = ((shz - D.glo_hi[2]) + (slz - D.glo_lo[2])) * D.inv_f[2] - (float)cbz;
+    } else {
+        fx = (float)(__dmul_rn(sx - D.glo[0], D.inv[0]) - (double)cbx);
+        fy = (float)(__dmul_rn(sy - D.glo[1], D.inv[1]) - (double)cby);
+        fz = (float)(__dmul_rn(sz - D.glo[2], D.inv[2]) - (double)cbz);
+    }
     const bool near_ok = fx >= -1e-3f && fx <= 1.001f && fy >= -1e-3f && fy <= 1.001f && fz >= -1e-3f &&
-                         fz <= 1.001f && D.min_size > 0.0;
-    const float bsx = (float)D.size[0], bsy = (float)D.size[1], bsz = (float)D.size[2];
+                         fz <= 1.001f && D.has_extent;
+    const float bsx = D.size_f[0], bsy = D.size_f[1], bsz = D.size_f[2];
+    const float feps = D.frac_eps;
     // squared distance (bin units scaled by the bin sides) from the site to
-    // the nearest point of the bin at offset (i, j, k)
+    // the nearest point of the bin at offset (i, j, k), each gap shortened by
+    // the in-bin position's error bound
     auto near2 = [&](int i, int j, int k) -> float {
         const float fxc = fminf(fmaxf(fx, 0.f), 1.f), fyc = fminf(fmaxf(fy, 0.f), 1.f),
                     fzc = fminf(fmaxf(fz, 0.f), 1.f);
-        const float dx = i > 0 ? (float)i - fxc : (i < 0 ? (float)(-i - 1) + fxc : 0.f);
-        const float dy = j > 0 ? (float)j - fyc : (j < 0 ? (float)(-j - 1) + fyc : 0.f);
-        const float dz = k > 0 ? (float)k - fzc : (k < 0 ? (float)(-k - 1) + fzc : 0.f);
+        const float dx = i > 0 ? fmaxf((float)i - fxc - feps, 0.f) : (i < 0 ? fmaxf((float)(-i - 1) + fxc - feps, 0.f) : 0.f);
+        const float dy = j > 0 ? fmaxf((float)j - fyc - feps, 0.f) : (j < 0 ? fmaxf((float)(-j - 1) + fyc - feps, 0.f) : 0.f);
+        const float dz = k > 0 ? fmaxf((float)k - fzc - feps, 0.f) : (k < 0 ? fmaxf((float)(-k - 1) + fzc - feps, 0.f) : 0.f);
         const float ax = dx * bsx, ay = dy * bsy, az = dz * bsz;
         return ax * ax + ay * ay + az * az;
     };
@@ -1365,7 +1451,64 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         __syncwarp();
         bool bad = fbad;
         double vpart = 0.0;
-        if constexpr (GUARD) {
+        if constexpr (GUARD && !EXACT) {
+            // Face planes as FP32 pairs, without the FP64 pipe: the bisector of
+            // the site and point q has n = q = p_j - site and h = q.q / 2
+            // (vector3.rs:223-239 up to the scale of n).  q comes from the
+            // points' FP32 pairs (hi + lo relative to the centre, 48 bits) by a
+            // TwoSum of the high parts, so its error is ~2^-46 of the
+            // distance from the centre; h = q.q / 2 follows in double-float.
+            // Walls: n = +-e_a, h = the distance to the wall (FP64; only cells
+            // that touch a wall have such faces).
+            const double* blo = P.box_override ? P.box : D.blo;
+            const double* bhi = P.box_override ? P.box + 3 : D.bhi;
+            for (int p = lane; p < C.np; p += 32) {
+                if (S.fdeg[p] == 0) continue;
+                float q0, q1, q2, l0 = 0.f, l1 = 0.f, l2 = 0.f, hh, hl, dist;
+                if (p < 6) {
+                    const int a = p >> 1;
+                    const bool mx = p & 1;
+                    const double s_a = a == 0 ? sx : (a == 1 ? sy : sz);
+                    const double h = mx ? (bhi[a] - s_a) : (s_a - blo[a]);
+                    hh = (float)h;
+                    hl = (float)(h - (double)hh);
+                    q0 = a == 0 ? (mx ? 1.f : -1.f) : 0.f;
+                    q1 = a == 1 ? (mx ? 1.f : -1.f) : 0.f;
+                    q2 = a == 2 ? (mx ? 1.f : -1.f) : 0.f;
+                    dist = hh;
+                } else {
+                    const uint32_t j = S.psrc[p];
+                    float sh, se;
+                    two_sum(P.shi[3ull * j], -shx, sh, se);
+                    two_sum(sh, (P.slo[3ull * j] - slx) + se, q0, l0);
+                    two_sum(P.shi[3ull * j + 1], -shy, sh, se);
+                    two_sum(sh, (P.slo[3ull * j + 1] - sly) + se, q1, l1);
+                    two_sum(P.shi[3ull * j + 2], -shz, sh, se);
+                    two_sum(sh, (P.slo[3ull * j + 2] - slz) + se, q2, l2);
+                    float p0, e0, p1, e1, p2, e2, s01, t01, s2, t2;
+                    two_prod(q0, q0, p0, e0);
+                    two_prod(q1, q1, p1, e1);
+                    two_prod(q2, q2, p2, e2);
+                    two_sum(p0, p1, s01, t01);
+                    two_sum(s01, p2, s2, t2);
+                    const float low = ((e0 + e1) + e2) + (t01 + t2) + 2.f * (q0 * l0 + q1 * l1 + q2 * l2);
+                    float H, HL;
+                    two_sum(s2, low, H, HL);
+                    hh = 0.5f * H;   // exact scalings
+                    hl = 0.5f * HL;
+                    dist = 0.5f * sqrtf(H);
+                }
+                S.fqx[p] = q0;
+                S.fqy[p] = q1;
+                S.fqz[p] = q2;
+                S.qlx[p] = l0;
+                S.qly[p] = l1;
+                S.qlz[p] = l2;
+                S.qhh[p] = hh;
+                S.qhl[p] = hl;
+                S.qdist[p] = dist;
+            }
+        } else if constexpr (GUARD) {
             // FP64 face planes: bisector of the site and point q, n = q,
             // h = q.q / 2 (vector3.rs:223-239 up to the scale of n); walls
             // n = +-e_a, h = distance to the wall.
@@ -1402,11 +1545,30 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 S.fqz[p] = (float)qz;
                 S.qdist[p] = dist;
             }
+        }
+        if constexpr (GUARD) {
             __syncwarp();
             // One Newton step per vertex: residuals of its three planes in
-            // FP64, correction solved in FP32 (Cramer).  A correction larger
-            // than verify_rel * R means the FP32 vertex was not trustworthy:
-            // the cell re-runs in FP64.
+            // double-float (FP32 form) or FP64 (FP64-accurate finish),
+            // correction solved in FP32 (Cramer).  A correction larger than
+            // verify_rel * R means the FP32 vertex was not trustworthy: the
+            // cell re-runs in FP64.
+            // The residual h - n.x of a plane kept as FP32 pairs: the high
+            // parts' products exact (FMA), summed by TwoSum, the low-order
+            // terms in FP32; accurate to ~2^-46 |n| |x|, far below the
+            // residual of an FP32 vertex (~1e-7 |n| |x|).
+            auto resid = [&](int pl, float x, float y, float z) -> float {
+                float p0, e0, p1, e1, p2, e2, s1, t1, s2, t2, s3, t3;
+                two_prod(S.fqx[pl], x, p0, e0);
+                two_prod(S.fqy[pl], y, p1, e1);
+                two_prod(S.fqz[pl], z, p2, e2);
+                two_sum(S.qhh[pl], -p0, s1, t1);
+                two_sum(s1, -p1, s2, t2);
+                two_sum(s2, -p2, s3, t3);
+                const float low = ((S.qhl[pl] - e0) - e1) - e2 + ((t1 + t2) + t3) -
+                                  (S.qlx[pl] * x + S.qly[pl] * y + S.qlz[pl] * z);
+                return s3 + low;
+            };
             const float vlim = P.verify_rel * sqrtf((float)R2);
 #pragma unroll
             for (int k = 0; k < K; ++k) {
@@ -1415,9 +1577,16 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     const uint32_t tt = S.tri[s];
                     const int a = plane_of(tt, 0), b = plane_of(tt, 1), c = plane_of(tt, 2);
                     const double x = (double)C.vx[k], y = (double)C.vy[k], z = (double)C.vz[k];
-                    const float ra = (float)(S.qh[a] - (S.qx[a] * x + S.qy[a] * y + S.qz[a] * z));
-                    const float rb = (float)(S.qh[b] - (S.qx[b] * x + S.qy[b] * y + S.qz[b] * z));
-                    const float rc = (float)(S.qh[c] - (S.qx[c] * x + S.qy[c] * y + S.qz[c] * z));
+                    float ra, rb, rc;
+                    if constexpr (EXACT) {
+                        ra = (float)(S.qh[a] - (S.qx[a] * x + S.qy[a] * y + S.qz[a] * z));
+                        rb = (float)(S.qh[b] - (S.qx[b] * x + S.qy[b] * y + S.qz[b] * z));
+                        rc = (float)(S.qh[c] - (S.qx[c] * x + S.qy[c] * y + S.qz[c] * z));
+                    } else {
+                        ra = resid(a, C.vx[k], C.vy[k], C.vz[k]);
+                        rb = resid(b, C.vx[k], C.vy[k], C.vz[k]);
+                        rc = resid(c, C.vx[k], C.vy[k], C.vz[k]);
+                    }
                     const float ax_ = S.fqx[a], ay_ = S.fqy[a], az_ = S.fqz[a];
                     const float bx_ = S.fqx[b], by_ = S.fqy[b], bz_ = S.fqz[b];
                     const float cx_ = S.fqx[c], cy_ = S.fqy[c], cz_ = S.fqz[c];

@@ -80,7 +80,24 @@ __global__ void k_grid_params(GridBuffers g) {
         D.size[a] = __ddiv_rn(ext, c);
         D.inv[a] = __ddiv_rn(c, ext);
         if (D.size[a] > 0.0) m = fmin(m, D.size[a]);
+        // FP32 forms for the FP32 clipping pass: offsets from the centre as
+        // FP32 pairs (48 bits), the bin sides and their inverses
+        const double gl = lo - D.ctr[a], bl = D.blo[a] - D.ctr[a], bh = D.bhi[a] - D.ctr[a];
+        D.glo_hi[a] = __double2float_rn(gl);
+        D.glo_lo[a] = __double2float_rn(gl - (double)D.glo_hi[a]);
+        D.blo_hi[a] = __double2float_rn(bl);
+        D.blo_lo[a] = __double2float_rn(bl - (double)D.blo_hi[a]);
+        D.bhi_hi[a] = __double2float_rn(bh);
+        D.bhi_lo[a] = __double2float_rn(bh - (double)D.bhi_hi[a]);
+        D.inv_f[a] = __double2float_rn(D.inv[a]);
+        D.size_f[a] = __double2float_rn(D.size[a]);
     }
+    D.rcp_cpd = 1.0f / (float)D.cpd;
+    D.rcp_cpd2 = 1.0f / ((float)D.cpd * (float)D.cpd);
+    // (x - glo) * inv from the FP32 pairs: one rounding of the difference, one
+    // of inv, one of the product (u = 2^-24 each, relative to the result, at
+    // most cpd bins), with a factor 4 in hand
+    D.frac_eps = 4.0f * 5.9604645e-8f * (float)D.cpd + 1e-6f;
     // Table extent: every offset whose key is <= (gaps * m)^2 has all gap
     // counts <= gaps, hence |offset| <= gaps + 1 on every axis.
     int cheb = g.table_gaps + 1;
@@ -90,6 +107,7 @@ __global__ void k_grid_params(GridBuffers g) {
     // The table holds every offset of the grid when that fits; otherwise the
     // offsets with key <= kmax, and the walk continues ring by ring.
     const bool complete = cheb == D.cpd - 1 && (2 * cheb + 1) * (2 * cheb + 1) * (2 * cheb + 1) <= kMaxTable;
+    D.has_extent = m != DBL_MAX;
     if (m == DBL_MAX) {          // every point identical: only the own bin holds points
         D.min_size = 0.0;
         D.tab_kmax = INFINITY;

@@ -55,6 +55,17 @@ struct DiagDesc {
     uint32_t tab_cap;        // table capacity reserved by the host
     int32_t cpd;             // cells_per_dimension (host, glibc cbrt)
     int32_t cheb;            // Chebyshev radius enumerated into the table
+    // FP32 forms of the grid and the box for the FP32 clipping pass (device-
+    // written with the grid): offsets from ctr as FP32 pairs (hi + lo), so the
+    // site's place in its bin and the box corners come out of FP32 arithmetic
+    float glo_hi[3], glo_lo[3];          // point bounds' low corner - ctr
+    float blo_hi[3], blo_lo[3];          // container box low corner - ctr
+    float bhi_hi[3], bhi_lo[3];          // container box high corner - ctr
+    float inv_f[3];                      // inverse bin sides
+    float size_f[3];                     // bin sides
+    float rcp_cpd, rcp_cpd2;             // 1 / cpd, 1 / cpd^2 (bin id -> coordinates)
+    float frac_eps;                      // bound on the FP32 in-bin position's error, in bins
+    int32_t has_extent;                  // some bin side is nonzero (min_size > 0)
 };
 
 // Shell-table entry: a bin offset and its search-order key (celery.rs:423-427)
@@ -233,6 +244,7 @@ struct ClipParams {
     const uint32_t* delims;
     const uint32_t* sgroup;
     const TabEntry* table;
+    const uint32_t* bin;            // global bin of each point (original order)
     // work: sorted positions to process
     const uint32_t* work;          // null: 0 .. total-1
     const uint32_t* work_count;    // null: total
