@@ -121,6 +121,9 @@ struct Engine {
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // the binning pass builds the shell tables on a side stream (fork/join)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     size_t ndiag = 0;
     uint32_t total = 0;
     uint64_t total_bins = 0;
@@ -250,6 +253,11 @@ struct Engine {
         dfree(d_sample); dfree(d_occ);
         if (own_stream && stream) cudaStreamDestroy(stream);
         stream = nullptr;
+        if (side) cudaStreamDestroy(side);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        side = nullptr;
+        ev_fork = ev_join = nullptr;
     }
 
     int blocks(int precision, int slots, int form = kFormStd) {
@@ -348,6 +356,9 @@ tess_status engine_init(Engine& E, const tess_config* cfg, std::vector<DiagDesc>
         CU(cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking));
         E.own_stream = true;
     }
+    CU(cudaStreamCreateWithFlags(&E.side, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&E.ev_fork, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&E.ev_join, cudaEventDisableTiming));
     E.ndiag = diags.size();
     uint64_t total = 0, bins = 0, tab = 0;
     std::vector<uint32_t> cdiag, cstart;
@@ -454,7 +465,7 @@ tess_status engine_build(Engine& E, bool check) {
         CU(ev.create(2));
         CU(cudaEventRecord(ev.e[0], E.stream));
     }
-    CU(launch_grid_build(grid_buffers(E), E.stream));
+    CU(launch_grid_build(grid_buffers(E), E.stream, E.side, E.ev_fork, E.ev_join));
     E.launches += kGridLaunches;
     if (timing) CU(cudaEventRecord(ev.e[1], E.stream));
     if (check) {
@@ -1632,7 +1643,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
         cudaGraph_t g = nullptr;
         CU(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
         tess_status st = TESS_OK;
-        cudaError_t ce = launch_grid_build(grid_buffers(E), E.stream);
+        cudaError_t ce = launch_grid_build(grid_buffers(E), E.stream, E.side, E.ev_fork, E.ev_join);
         if (ce != cudaSuccess) st = fail(TESS_E_CUDA, "capture: %s", cudaGetErrorString(ce));
         if (st == TESS_OK) st = enqueue_passes(E, prec, -1.0, -1, false, nullptr);
         cudaError_t ee = cudaStreamEndCapture(E.stream, &g);

@@ -14,52 +14,107 @@ namespace {
 
 constexpr int kBoundsThreads = 256;
 
-__device__ __forceinline__ double warp_min(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+// The pass runs on the integer pipes: on this part an FP64 instruction costs
+// dozens of issue slots' worth of pipe time, which made the FP64 forms of the
+// bounds, the bin formula and the split bound the pass by the FP64 pipe.
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
-__device__ __forceinline__ double warp_max(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
 
-// CeleryBounds::new (celery.rs:81-125): per-chunk min/max, merged with
-// order-preserving 64-bit atomics.  Non-finite inputs raise error_flag.
+// CeleryBounds::new (celery.rs:81-125): per-chunk min/max of the coordinates'
+// order-preserving integer codes (ord_enc: the same order as the doubles),
+// merged with 64-bit atomics.  Non-finite inputs (exponent all ones) raise
+// error_flag.
 __global__ void __launch_bounds__(kBoundsThreads) k_bounds(GridBuffers g) {
-    __shared__ double red[6][kBoundsThreads / 32];
+    __shared__ unsigned long long red[6][kBoundsThreads / 32];
     for (uint32_t c = blockIdx.x; c < g.nchunks; c += gridDim.x) {
         const uint32_t d = g.chunk_diag[c];
         const uint32_t beg = g.chunk_start[c];
         const DiagDesc& D = g.diags[d];
         const uint32_t end = min(beg + kChunk, D.pt_base + D.n);
-        double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX};
-        double mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+        unsigned long long mn[3] = {~0ull, ~0ull, ~0ull};
+        unsigned long long mx[3] = {0ull, 0ull, 0ull};
         bool bad = false;
         for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
             for (int a = 0; a < 3; ++a) {
-                double v = g.xyz[3ull * i + a];
-                bad |= !isfinite(v);
-                mn[a] = fmin(mn[a], v);
-                mx[a] = fmax(mx[a], v);
+                const unsigned long long b = (unsigned long long)__double_as_longlong(g.xyz[3ull * i + a]);
+                bad |= ((b >> 52) & 0x7FFull) == 0x7FFull;
+                const unsigned long long e = (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+                mn[a] = min(mn[a], e);
+                mx[a] = max(mx[a], e);
             }
         }
         if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(g.error_flag, 1);
         const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
         for (int a = 0; a < 3; ++a) {
-            double lo = warp_min(mn[a]), hi = warp_max(mx[a]);
+            const unsigned long long lo = warp_min_u64(mn[a]), hi = warp_max_u64(mx[a]);
             if (l == 0) { red[a][w] = lo; red[3 + a][w] = hi; }
         }
         __syncthreads();
         if (threadIdx.x < 6) {
             const int a = threadIdx.x;
-            double v = red[a][0];
-            for (int k = 1; k < kBoundsThreads / 32; ++k) v = a < 3 ? fmin(v, red[a][k]) : fmax(v, red[a][k]);
-            unsigned long long e = ord_enc(v);
-            if (a < 3) atomicMin(&g.bounds[6 * d + a], e);
-            else atomicMax(&g.bounds[6 * d + a], e);
+            unsigned long long v = red[a][0];
+            for (int k = 1; k < kBoundsThreads / 32; ++k) v = a < 3 ? min(v, red[a][k]) : max(v, red[a][k]);
+            if (a < 3) atomicMin(&g.bounds[6 * d + a], v);
+            else atomicMax(&g.bounds[6 * d + a], v);
         }
         __syncthreads();
     }
+}
+
+// x rounded toward zero to FP32 by integer operations (within 2^-23 |x|).
+// False for zeros, subnormals, non-finite values and magnitudes outside
+// FP32's normal range: those take the exact FP64 formula.
+__device__ __forceinline__ bool f32_trunc(double x, float& f) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t hi = (uint32_t)(b >> 32);
+    const int e = (int)((hi >> 20) & 0x7FFu);
+    const int fe = e - 1023 + 127;
+    if (e == 0 || e == 0x7FF || fe < 1 || fe > 254) return false;
+    f = __uint_as_float((hi & 0x80000000u) | ((uint32_t)fe << 23) | (uint32_t)((b >> 29) & 0x7FFFFFull));
+    return true;
+}
+
+// axis_index (celery.rs:269-314) without the FP64 pipe for nearly every point:
+// x >= max is decided on the order-preserving codes (exact), and
+// v = (x - min) * inv by an FP32 estimate t with a bound E on |t - v|:
+//   x to FP32 by truncation (2^-23 |x|), min and inv rounded (2^-24 each),
+//   the difference and the product rounded (2^-24 each), and v's own two
+//   FP64 roundings (2^-52 each), so
+//   |t - v| <= inv (2^-23 |x| + 2^-24 |min|) + 3.1 * 2^-24 |t|,
+// which E = inv (|x| + |min|) 2^-22 + |t| 2^-21 covers twice over.  When
+// [t - E, t + E] holds no integer (nor 0, nor cpd - 1) the bin is the one
+// the FP64 formula gives; otherwise (a point within E of a bin boundary,
+// about 2 * 10^-4 of a bin for the unit cube at cpd = 238) ok is false and
+// the caller uses the FP64 formula.
+__device__ __forceinline__ int axis_index_fast(double x, const DiagDesc& D, int a, int cpd, bool& ok) {
+    const unsigned long long xb = (unsigned long long)__double_as_longlong(x);
+    float xf;
+    if (!f32_trunc(x, xf)) {
+        ok = false;
+        return 0;
+    }
+    const unsigned long long hb = (unsigned long long)__double_as_longlong(D.ghi[a]);
+    const unsigned long long xe = (xb >> 63) ? ~xb : (xb | 0x8000000000000000ull);
+    const unsigned long long he = (hb >> 63) ? ~hb : (hb | 0x8000000000000000ull);
+    if (xe >= he) return cpd - 1;
+    const float lf = D.glo_f[a], inv = D.inv_f[a];
+    const float t = (xf - lf) * inv;
+    const float E = inv * (fabsf(xf) + fabsf(lf)) * 2.3841858e-7f + fabsf(t) * 4.7683716e-7f;
+    const float up = t + E;
+    if (up < 1.0f) return 0;                      // v < 1: 0 (v <= 0 gives 0 too)
+    const float dn = t - E;
+    if (dn >= (float)(cpd - 1)) return cpd - 1;   // v >= cpd - 1
+    const float fl = floorf(dn);
+    if (dn > 0.f && fl == floorf(up)) return (int)fl;
+    ok = false;
+    return 0;
 }
 
 // CeleryCellInfo::new (celery.rs:153-181) from the bounds and the host's cpd.
@@ -90,6 +145,7 @@ __global__ void k_grid_params(GridBuffers g) {
         D.bhi_hi[a] = __double2float_rn(bh);
         D.bhi_lo[a] = __double2float_rn(bh - (double)D.bhi_hi[a]);
         D.inv_f[a] = __double2float_rn(D.inv[a]);
+        D.glo_f[a] = __double2float_rn(lo);
         D.size_f[a] = __double2float_rn(D.size[a]);
     }
     D.rcp_cpd = 1.0f / (float)D.cpd;
@@ -130,9 +186,14 @@ __global__ void k_bin_count(GridBuffers g) {
         const int cpd = D.cpd;
         for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
             const double x = g.xyz[3ull * i], y = g.xyz[3ull * i + 1], z = g.xyz[3ull * i + 2];
-            const int bx = axis_index(x, D.glo[0], D.ghi[0], D.inv[0], cpd);
-            const int by = axis_index(y, D.glo[1], D.ghi[1], D.inv[1], cpd);
-            const int bz = axis_index(z, D.glo[2], D.ghi[2], D.inv[2], cpd);
+            bool okx = true, oky = true, okz = true;
+            int bx = axis_index_fast(x, D, 0, cpd, okx);
+            int by = axis_index_fast(y, D, 1, cpd, oky);
+            int bz = axis_index_fast(z, D, 2, cpd, okz);
+            // the exact FP64 formula for the few coordinates near a boundary
+            if (!okx) bx = axis_index(x, D.glo[0], D.ghi[0], D.inv[0], cpd);
+            if (!oky) by = axis_index(y, D.glo[1], D.ghi[1], D.inv[1], cpd);
+            if (!okz) bz = axis_index(z, D.glo[2], D.ghi[2], D.inv[2], cpd);
             // get_cell_from_indices, celery.rs:317-325
             const uint64_t b = D.bin_base + ((uint64_t)bx * cpd + by) * cpd + bz;
             g.bin[i] = (uint32_t)b;
@@ -304,6 +365,41 @@ __global__ void __launch_bounds__(256) k_bin_order(GridBuffers g) {
     }
 }
 
+// hi = u rounded to FP32 (to nearest, ties to even) and lo = u - hi rounded to
+// FP32, by integer operations on u's bits: the same values as
+// __double2float_rn(u) and __double2float_rn(u - (double)hi).  u - hi is
+// exact in units of 2^(E - 52) (at most 29 bits), so one integer-to-FP32
+// rounding and an exact power-of-two scale give lo.  False (the FP64 form
+// then runs) when lo would be subnormal or hi leaves FP32's normal range.
+__device__ __forceinline__ bool split_rn_int(double u, float& hi, float& lo) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(u);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7FFull);
+    if (e == 0) {
+        if ((b << 1) != 0) return false;          // subnormal
+        hi = __uint_as_float(sign);               // +-0: lo = +0 as u - hi is +0
+        lo = 0.f;
+        return true;
+    }
+    if (e == 0x7FF) return false;
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    unsigned long long q = m >> 29;
+    const unsigned long long rem = m & ((1ull << 29) - 1);
+    if (rem > (1ull << 28) || (rem == (1ull << 28) && (q & 1ull))) q += 1;
+    const long long diff = (long long)m - (long long)(q << 29);
+    int ehi = e;
+    if (q == (1ull << 24)) {
+        q >>= 1;
+        ehi += 1;
+    }
+    const int fe = ehi - 1023 + 127;
+    const int pe = e - 1023 - 52 + 127;
+    if (fe < 1 || fe > 254 || (diff != 0 && pe < 1)) return false;
+    hi = __uint_as_float(sign | ((uint32_t)fe << 23) | ((uint32_t)q & 0x7FFFFFu));
+    lo = diff == 0 ? 0.f : __ll2float_rn(sign ? -diff : diff) * __uint_as_float((uint32_t)pe << 23);
+    return true;
+}
+
 // Positions (and groups) in sorted order, SoA for coalesced candidate loads.
 // The FP32 pair (hi, lo) splits the position relative to its diagram's
 // centre: the split keeps 48 bits of that offset, so its error scales with
@@ -324,14 +420,16 @@ __global__ void k_gather(GridBuffers g) {
         else hi = mid - 1;
     }
     const DiagDesc& D = g.diags[lo];
-    const double ux = x - D.ctr[0], uy = y - D.ctr[1], uz = z - D.ctr[2];
-    const float hx = __double2float_rn(ux), hy = __double2float_rn(uy), hz = __double2float_rn(uz);
-    g.shi[3ull * s] = hx;
-    g.shi[3ull * s + 1] = hy;
-    g.shi[3ull * s + 2] = hz;
-    g.slo[3ull * s] = __double2float_rn(ux - (double)hx);
-    g.slo[3ull * s + 1] = __double2float_rn(uy - (double)hy);
-    g.slo[3ull * s + 2] = __double2float_rn(uz - (double)hz);
+    const double u[3] = {x - D.ctr[0], y - D.ctr[1], z - D.ctr[2]};
+    for (int a = 0; a < 3; ++a) {
+        float h, l;
+        if (!split_rn_int(u[a], h, l)) {
+            h = __double2float_rn(u[a]);
+            l = __double2float_rn(u[a] - (double)h);
+        }
+        g.shi[3ull * s + a] = h;
+        g.slo[3ull * s + a] = l;
+    }
     if (g.sgroup) g.sgroup[s] = g.groups[i];
 }
 
@@ -454,7 +552,8 @@ cudaError_t launch_occupancy(const uint32_t* delims, uint64_t nbins, uint32_t cr
 // Binning pass: bounds -> grid parameters -> shell tables -> histogram ->
 // scan -> scatter -> within-bin order -> gather.  A fixed launch sequence
 // (no host synchronisation), so it can be captured in a CUDA graph.
-cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s) {
+cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s, cudaStream_t side, cudaEvent_t fork,
+                              cudaEvent_t join) {
     const int ndiag = g.ndiag;
     k_bounds_init<<<(6 * ndiag + 255) / 256, 256, 0, s>>>(g.bounds, ndiag);
     cudaMemsetAsync(g.delims, 0, sizeof(uint32_t) * (g.total_bins + 1), s);
@@ -462,7 +561,17 @@ cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s) {
     const int cblocks = (int)(g.nchunks < 4096u ? g.nchunks : 4096u);
     k_bounds<<<cblocks, kBoundsThreads, 0, s>>>(g);
     k_grid_params<<<(ndiag + 127) / 128, 128, 0, s>>>(g);
-    k_table<<<ndiag, kTabThreads, 0, s>>>(g);
+    // the shell tables need only the grid parameters: build them beside the
+    // histogram, scan and scatter when a side stream is given
+    const bool forked = side && fork && join;
+    if (forked) {
+        cudaEventRecord(fork, s);
+        cudaStreamWaitEvent(side, fork, 0);
+        k_table<<<ndiag, kTabThreads, 0, side>>>(g);
+        cudaEventRecord(join, side);
+    } else {
+        k_table<<<ndiag, kTabThreads, 0, s>>>(g);
+    }
     k_bin_count<<<cblocks, 256, 0, s>>>(g);
     const uint64_t nscan = g.total_bins + 1;
     const uint64_t per = (uint64_t)kScanThreads * kScanItems;
@@ -473,6 +582,7 @@ cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s) {
     k_scatter<<<(g.total + 255) / 256, 256, 0, s>>>(g);
     k_bin_order<<<(unsigned)((g.total_bins + 255) / 256), 256, 0, s>>>(g);
     k_gather<<<(g.total + 255) / 256, 256, 0, s>>>(g);
+    if (forked) cudaStreamWaitEvent(s, join, 0);
     return cudaGetLastError();
 }
 

@@ -62,6 +62,7 @@ struct DiagDesc {
     float blo_hi[3], blo_lo[3];          // container box low corner - ctr
     float bhi_hi[3], bhi_lo[3];          // container box high corner - ctr
     float inv_f[3];                      // inverse bin sides
+    float glo_f[3];                      // point bounds' low corner, rounded to FP32
     float size_f[3];                     // bin sides
     float rcp_cpd, rcp_cpd2;             // 1 / cpd, 1 / cpd^2 (bin id -> coordinates)
     float frac_eps;                      // bound on the FP32 in-bin position's error, in bins
@@ -154,7 +155,11 @@ constexpr uint32_t kChunk = 8192;
 constexpr int kScanItems = 8;       // items per thread in the scan
 constexpr int kScanThreads = 1024;
 
-cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s);
+// side/fork/join (optional): a second stream and two events; the shell
+// table is then built on the side stream while the histogram, scan and
+// scatter run (fork after the grid parameters, join before returning).
+cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s, cudaStream_t side = nullptr,
+                              cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 // out[0] = most points in one bin, out[1] = points in bins of >= crowd points
 // (every bin of every diagram of the set)
 cudaError_t launch_occupancy(const uint32_t* delims, uint64_t nbins, uint32_t crowd, unsigned long long* out,
