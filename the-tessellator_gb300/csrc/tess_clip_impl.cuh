@@ -99,6 +99,7 @@ struct Smem {
             T px[P], py[P], pz[P], pd[P];     // plane: normal, offset (n.x = offset)
             T pn[P];                          // |normal| (1 for the FP64 form and the walls)
             T vsd[V];                         // signed distances of the current cut
+            T vr[V];                          // (|v| + e_v)^2 of each slot (FP32), |v|^2 (FP64)
             uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
             uint32_t cbeg2[32], ccnt[32];     // second-half bins: starts and prefix counts
             uint32_t pused[(P + 31) / 32];    // plane recycling: planes referenced by live vertices
@@ -286,6 +287,14 @@ __device__ __forceinline__ void bisector(double rx, double ry, double rz, double
 
 __device__ __forceinline__ float round_up_f(float x) { return x; }
 __device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
+
+// A vertex's share of the cell radius: (|v| + e_v)^2 in the FP32 form (|v|
+// from the upper-bound root), |v|^2 in the FP64 form.
+__device__ __forceinline__ float vrad2(float x, float y, float z, float e) {
+    const float r = sqrt_up(x * x + y * y + z * z) + e;
+    return r * r;
+}
+__device__ __forceinline__ double vrad2(double x, double y, double z, double) { return x * x + y * y + z * z; }
 
 // Per-warp work counters (reported when ClipParams::work_ctr is set).  The
 // lean first-pass form does not count: the registers cost it 2%.
@@ -493,6 +502,7 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
             S.vy[slot] = py;
             S.vz[slot] = pz;
             if constexpr (GUARD) S.ve[slot] = pe;
+            S.vr[slot] = vrad2(px, py, pz, pe);
             S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
             // Y's pointer back to X is the edge (b, a) of Y's triple.
             const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
@@ -799,6 +809,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             S.vy[slot] = py;
             S.vz[slot] = pz;
             if constexpr (GUARD) S.ve[slot] = pe;
+            S.vr[slot] = vrad2(px, py, pz, pe);
             S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
             // Y's pointer back to X is the edge (b, a) of Y's triple.
             const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
@@ -859,21 +870,16 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
 }
 
 // Squared radius of the cell about its site: max |v|^2 over live vertices;
-// in the FP32 form each |v| is inflated by its error bound.
+// in the FP32 form each |v| is inflated by its error bound.  Each slot's term
+// (vrad2) is written with the vertex, so a cut costs one load per register
+// set here instead of a square root per vertex.
 template <typename T, int K>
-__device__ __forceinline__ T live_r2(const CellRegs<T, K>& C, int lane) {
+__device__ __forceinline__ T live_r2(const Smem<T, K>& S, const CellRegs<T, K>& C, int lane) {
     T r2 = 0;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         if (C.lm[k] == 0) continue;
-        if ((C.lm[k] >> lane) & 1u) {
-            T q = C.vx[k] * C.vx[k] + C.vy[k] * C.vy[k] + C.vz[k] * C.vz[k];
-            if (sizeof(T) == 4) {
-                const T r = sqrt_up(q) + C.ve[k];
-                q = r * r;
-            }
-            r2 = max(r2, q);
-        }
+        if ((C.lm[k] >> lane) & 1u) r2 = max(r2, S.vr[k * 32 + lane]);
     }
     if constexpr (sizeof(T) == 4) {
         // r2 >= 0 and never NaN (max drops NaN): its bits order like its
@@ -1018,6 +1024,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             C.ve[0] = ((T)(kF32Setup ? 2.5e-7 : 1.2e-7) + (T)P.guard_rel) * (fabs(C.vx[0]) + fabs(C.vy[0]) + fabs(C.vz[0]));
             S.ve[lane] = C.ve[0];
         }
+        S.vr[lane] = vrad2(C.vx[0], C.vy[0], C.vz[0], C.ve[0]);
         const int pX = bx, pY = 2 + by, pZ = 4 + bz;
         const int sgn = (bx ? 1 : -1) * (by ? 1 : -1) * (bz ? 1 : -1);
         const int t0 = pX, t1 = sgn > 0 ? pY : pZ, t2 = sgn > 0 ? pZ : pY;
@@ -1035,7 +1042,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     C.nfree = S_t::VUSE - 8;
     for (int i = lane; i < C.nfree; i += 32) S.fl[i] = (uint8_t)(S_t::VUSE - 1 - i);
     __syncwarp();
-    T R2 = live_r2(C, lane);
+    T R2 = live_r2(S, C, lane);
     // guard_rel * cell radius: the hybrid form's limit on a vertex's error bound
     T cR = (T)P.guard_rel * sqrt_up(R2);
     // FP32 form, the hi/lo split's share of a plane test's error (u = 2^-24,
@@ -1153,7 +1160,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     W.newv += (unsigned)(r - 1);
                 }
                 const T R2b = R2;
-                R2 = live_r2(C, lane);
+                R2 = live_r2(S, C, lane);
                 cR = (T)P.guard_rel * sqrt_up(R2);
                 // hybrid form: a cut never moves a vertex beyond the cell
                 // (convexity), so a radius that grew (or is no longer
@@ -1171,13 +1178,16 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         // candidate order: every first-half bin (nearer in the table) before
         // every second-half bin
         const unsigned inca = warp_incl_scan_u(cntA, lane);
-        const unsigned incb = warp_incl_scan_u(cntB, lane);
         const unsigned totala = __shfl_sync(FULL, inca, 31);
-        const unsigned total = totala + __shfl_sync(FULL, incb, 31);
+        unsigned total = totala;
         S.cpref[lane] = inca - cntA;
         S.cbeg[lane] = begA;
-        S.ccnt[lane] = totala + incb - cntB;   // prefix of the second-half bins
-        S.cbeg2[lane] = begB;
+        if constexpr (kBatch2) {
+            const unsigned incb = warp_incl_scan_u(cntB, lane);
+            total += __shfl_sync(FULL, incb, 31);
+            S.ccnt[lane] = totala + incb - cntB;   // prefix of the second-half bins
+            S.cbeg2[lane] = begB;
+        }
         __syncwarp();
         for (unsigned w0 = 0; w0 < total; w0 += 32) {
             if constexpr (BASE != kFormLean) ++W.windows;
@@ -1189,7 +1199,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             const T lim = (T)4 * R2 * (T)kStopMargin;
             bool near = false;
             if (c < total) {
-                const bool second = c >= totala;
+                const bool second = kBatch2 && c >= totala;
                 const uint32_t* pref = second ? S.ccnt : S.cpref;
                 int lo = 0, hi = 31;
                 while (lo < hi) {
