@@ -58,8 +58,6 @@ constexpr unsigned FULL = 0xffffffffu;
 // FP32 form: relative error constant of a vertex solved from its three planes
 // (a few FP32 roundings of the plane data and of Cramer's rule).
 constexpr float kVertexErr = 1.5e-6f;
-// Shell-table entries per walk batch: 32 (one per lane) or 64 (two per lane).
-constexpr bool kBatch2 = false;
 // Load the next batch's table entries and bin ranges before cutting the
 // current batch (overlaps their latency, costs registers).
 constexpr bool kPrefetch = true;
@@ -101,7 +99,15 @@ struct Smem {
             T vsd[V];                         // signed distances of the current cut
             T vr[V];                          // (|v| + e_v)^2 of each slot (FP32), |v|^2 (FP64)
             uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
-            uint32_t cbeg2[32], ccnt[32];     // second-half bins: starts and prefix counts
+            uint32_t nbeg[32], ncnt[32];      // crowded bins: the 27 neighbour bins' ranges ...
+            float nd[32];                     // ... and the squared distance to their nearest point
+            uint32_t pending;                 // crowded bins still to handle (mask over the 27)
+            T sdx[32], sdy[32], sdz[32], sd2[32];   // each lane's seed: offset, squared length ...
+            uint32_t sdj[32];                 // ... sorted index (~0: none)
+            int32_t sdcid[32];                // ... and local original id
+            int32_t cbin;                     // the crowded bin being handled
+            int32_t ring;                     // Chebyshev ring being walked ...
+            uint32_t r0;                      // ... and the position in it
             uint32_t pused[(P + 31) / 32];    // plane recycling: planes referenced by live vertices
             float ve[VF];                     // vertex error bounds (mirror of CellRegs::ve)
             uint16_t items[V + 32];           // boundary edges of a cut: slot | edge << 8
@@ -1174,46 +1180,51 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
 
     // Cut by every point of the lane's two bins, given as sorted ranges
     // [begA, begA + cntA) and [begB, begB + cntB).
-    auto process = [&](unsigned begA, unsigned cntA, unsigned begB, unsigned cntB) -> int {
-        // candidate order: every first-half bin (nearer in the table) before
-        // every second-half bin
-        const unsigned inca = warp_incl_scan_u(cntA, lane);
-        const unsigned totala = __shfl_sync(FULL, inca, 31);
-        unsigned total = totala;
-        S.cpref[lane] = inca - cntA;
-        S.cbeg[lane] = begA;
-        if constexpr (kBatch2) {
-            const unsigned incb = warp_incl_scan_u(cntB, lane);
-            total += __shfl_sync(FULL, incb, 31);
-            S.ccnt[lane] = totala + incb - cntB;   // prefix of the second-half bins
-            S.cbeg2[lane] = begB;
+    // Cut by every point of the lanes' bins, given as sorted ranges
+    // [beg, beg + cnt), in lane order; or (direct) by one window of the
+    // lanes' seeds of a crowded bin (S.sd*).
+    auto process = [&](unsigned beg, unsigned cnt, bool direct) -> int {
+        unsigned total = 32;
+        if (!direct) {
+            const unsigned inc = warp_incl_scan_u(cnt, lane);
+            total = __shfl_sync(FULL, inc, 31);
+            S.cpref[lane] = inc - cnt;
+            S.cbeg[lane] = beg;
+            __syncwarp();
         }
-        __syncwarp();
         for (unsigned w0 = 0; w0 < total; w0 += 32) {
-            if constexpr (BASE != kFormLean) ++W.windows;
-            const unsigned c = w0 + lane;
             bool keep = false;
             T rx = 0, ry = 0, rz = 0, r2 = 0;
             uint32_t j = 0;
             int32_t cid = 0;
-            const T lim = (T)4 * R2 * (T)kStopMargin;
             bool near = false;
-            if (c < total) {
-                const bool second = kBatch2 && c >= totala;
-                const uint32_t* pref = second ? S.ccnt : S.cpref;
-                int lo = 0, hi = 31;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (pref[mid] <= c) lo = mid;
-                    else hi = mid - 1;
+            if (kSeedForm && direct) {
+                j = S.sdj[lane];
+                keep = j != 0xFFFFFFFFu;
+                rx = S.sdx[lane];
+                ry = S.sdy[lane];
+                rz = S.sdz[lane];
+                r2 = S.sd2[lane];
+                cid = S.sdcid[lane];
+            } else {
+                if constexpr (BASE != kFormLean) ++W.windows;
+                const unsigned c = w0 + lane;
+                const T lim = (T)4 * R2 * (T)kStopMargin;
+                if (c < total) {
+                    int lo = 0, hi = 31;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (S.cpref[mid] <= c) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    j = S.cbeg[lo] + (c - S.cpref[lo]);
+                    cand(j, rx, ry, rz, r2);
+                    keep = (j != self) && r2 > dup2 && r2 < lim;
+                    if constexpr (GUARD) near = (j != self) && !(r2 > dup2);
+                    if constexpr (kSeedForm) keep = keep && j != seedj;
+                    cid = (int32_t)(P.sorted[j] - pt_base);
+                    if (keep && tgroup >= 0) keep = (int64_t)(P.sgroup ? P.sgroup[j] : 0u) == tgroup;
                 }
-                j = (second ? S.cbeg2[lo] : S.cbeg[lo]) + (c - pref[lo]);
-                cand(j, rx, ry, rz, r2);
-                keep = (j != self) && r2 > dup2 && r2 < lim;
-                if constexpr (GUARD) near = (j != self) && !(r2 > dup2);
-                if constexpr (kSeedForm) keep = keep && j != seedj;
-                cid = (int32_t)(P.sorted[j] - pt_base);
-                if (keep && tgroup >= 0) keep = (int64_t)(P.sgroup ? P.sgroup[j] : 0u) == tgroup;
             }
             if (GUARD && __any_sync(FULL, near)) return ST_GUARD;
             const int st = run_window(keep, rx, ry, rz, r2, j, cid);
@@ -1263,11 +1274,18 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         return (long long)(bin_base + ((uint64_t)x * cpd + y) * cpd + z);
     };
 
-    // phase 1: the sorted shell table, 64 entries per batch (two per lane:
-    // entry t + lane and entry t + 32 + lane).  The next batch's table
-    // entries and bin ranges are loaded before the current batch's points are
-    // cut, so their latency overlaps the cutting.
-    bool phase2 = false;
+    // Phases of the walk:
+    //   0  crowded bins (seeded forms, when the site's own bin is crowded);
+    //   1  the sorted shell table, 32 entries per batch (one per lane); the
+    //      next batch's entries and bin ranges are loaded before the current
+    //      batch is cut, so their latency overlaps the cutting;
+    //   2  Chebyshev rings beyond the table (sparse regions).
+    // The seeded forms run them as one loop with one call of process(), so
+    // their window and cut code is inlined once: with a copy per phase,
+    // instruction fetch limited them (and the single loop takes their
+    // crowded-bin pass from 238 to 214 ms on the clustered 4M set).  The lean
+    // first pass keeps a loop per phase: it has no phase 0, and the single
+    // loop's dispatch made it 8% slower.
     uint32_t t = 0;
     // a batch entry: offsets, key and, after the bin test, the sorted range
     struct Ent {
@@ -1297,133 +1315,216 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             }
         }
     };
-    // ---- crowded bins first ----
+    int ph = 1;
+    if constexpr (!kSeedForm) {
+        Ent ea;
+        load_entry(lane, ea);
+        // lean first pass: a crowded own bin (table entry 0, lane 0's first
+        // entry) sends the cell to the seeded pass
+        if (BASE == kFormLean && P.list_dense && __shfl_sync(FULL, ea.cnt, 0) >= P.seed_min) status = ST_DENSE;
+        bool rings = false;
+        while (status == ST_OK) {
+            // The table key is rounded toward zero and the threshold up, so
+            // stopping on key >= thr never drops a bin that could hold a cutter.
+            const float thr = round_up_f((T)4 * R2 * (T)kStopMargin);
+            const unsigned ma = __ballot_sync(FULL, !(ea.key < thr));
+            const int na = ma ? __ffs(ma) - 1 : 32;
+            const unsigned ba = ea.beg;
+            unsigned ca = lane < na ? ea.cnt : 0u;
+            // re-test the bins against the current (smaller) radius
+            if (ca && near_ok && near2(ea.i, ea.j, ea.k) * (1.0f - 1e-4f) >= round_up_f((T)4 * R2)) ca = 0;
+            t += (uint32_t)na;
+            if (!ma) load_entry(t + lane, ea);
+            if constexpr (BASE != kFormLean) ++W.batches;
+            status = process(ba, ca, false);
+            if (status != ST_OK) break;
+            if (ma) {
+                rings = (t >= tab_len) && isfinite(D.tab_kmax);
+                break;
+            }
+        }
+        if (status == ST_OK && rings) {
+            for (int ring = 1; ring <= cpd - 1 && status == ST_OK; ++ring) {
+                double lbk = (double)(ring - 1) * D.min_size;
+                lbk = lbk * lbk;
+                if (lbk < D.tab_kmax) lbk = D.tab_kmax;
+                if (lbk >= 4.0 * (double)R2 * kStopMargin) break;
+                if (radius >= 0.0 && lbk > radius) break;
+                const uint32_t rs = 24u * (uint32_t)ring * (uint32_t)ring + 2u;
+                for (uint32_t r0 = 0; r0 < rs; r0 += 32) {
+                    const double thr = 4.0 * (double)R2 * kStopMargin;
+                    long long lb = -1;
+                    const uint32_t r = r0 + lane;
+                    if (r < rs) {
+                        int i, j, k;
+                        ring_offset(ring, r, i, j, k);
+                        const double key = gap_key(D.size, i, j, k);
+                        if (key > D.tab_kmax && key < thr && !(radius >= 0.0 && key > radius)) lb = bin_of(i, j, k);
+                    }
+                    if (!__any_sync(FULL, lb >= 0)) continue;
+                    if constexpr (BASE != kFormLean) ++W.batches;
+                    unsigned beg = 0, cnt = 0;
+                    if (lb >= 0) {
+                        beg = P.delims[lb];
+                        cnt = P.delims[lb + 1] - beg;
+                    }
+                    status = process(beg, cnt, false);
+                    if (status != ST_OK) break;
+                }
+            }
+        }
+        ph = 3;
+    }
+    // ---- phase 0: crowded bins first ----
     // When the site's own bin is crowded, it and every crowded neighbour bin
-    // still within reach are handled here one at a time, nearest first: the
-    // 32 seeds (the nearest point of each lane's stride of the bin) are cut
-    // nearest first, then the bin's windows, each lane skipping its own seed
-    // (window lane = position mod 32, the seed's stride).  The shell walk
-    // skips the bins done here (27-bit mask `done` over the offsets {-1,0,1}^3).
+    // still within reach are handled one at a time, nearest first, in two
+    // steps each: the 32 seeds (the nearest point of each lane's stride of
+    // the bin) are cut nearest first, then the bin's windows, each lane
+    // skipping its own seed (window lane = position mod 32, the seed's
+    // stride).  The shell walk skips the bins done here (27-bit mask `done`
+    // over the offsets {-1,0,1}^3).
+    // (their ranges and distances wait in shared memory: in registers they
+    // would stay live through every later cut)
+    bool seed_step = true;       // phase 0: the next step cuts a bin's seeds
     if constexpr (kSeedForm) {
         const uint64_t sb = bin_base + ((uint64_t)cbx * cpd + cby) * cpd + cbz;
         if (P.delims[sb + 1] - P.delims[sb] >= P.seed_min) {
             const int ti = lane / 9 - 1, tj = (lane / 3) % 3 - 1, tk = lane % 3 - 1;
-            unsigned nbeg = 0, ncnt = 0;
-            float nd = INFINITY;
+            unsigned nb = 0, nc = 0;
+            float dn = INFINITY;
             if (lane < 27) {
                 const long long lb = bin_of(ti, tj, tk);
                 if (lb >= 0 && !(has_radius && gap_key(D.size, ti, tj, tk) > radius)) {
-                    nbeg = P.delims[lb];
-                    ncnt = P.delims[lb + 1] - nbeg;
+                    nb = P.delims[lb];
+                    nc = P.delims[lb + 1] - nb;
                 }
-                nd = lane == 13 ? 0.f : (near_ok ? near2(ti, tj, tk) : INFINITY);
+                dn = lane == 13 ? 0.f : (near_ok ? near2(ti, tj, tk) : INFINITY);
             }
-            unsigned pending = __ballot_sync(FULL, ncnt >= P.seed_min && nd < INFINITY);
-            const unsigned ndkey = (__float_as_uint(nd) & ~31u) | (unsigned)lane;
-            while (pending && status == ST_OK) {
+            S.nbeg[lane] = nb;
+            S.ncnt[lane] = nc;
+            S.nd[lane] = dn;
+            S.pending = __ballot_sync(FULL, nc >= P.seed_min && dn < INFINITY);
+            ph = 0;
+        }
+    }
+    Ent ea;
+    bool loaded = false;                 // phase 1: the first batch is loaded
+    S.ring = 1;
+    S.r0 = 0;
+    while (kSeedForm && status == ST_OK) {
+        unsigned ba = 0, ca = 0;
+        bool direct = false;
+        if (kSeedForm && ph == 0) {
+            if (seed_step) {
+                const unsigned pending = S.pending;
+                if (!pending) {
+                    ph = 1;
+                    continue;
+                }
+                const unsigned ndkey = (__float_as_uint(S.nd[lane]) & ~31u) | (unsigned)lane;
                 const unsigned best = __reduce_min_sync(FULL, ((pending >> lane) & 1u) ? ndkey : 0xFFFFFFFFu);
-                const int t = (int)(best & 31u);
-                pending &= ~(1u << t);
+                const int cbin = (int)(best & 31u);
+                S.pending = pending & ~(1u << cbin);
+                S.cbin = cbin;
                 // still within reach of the (shrinking) cell?
-                if (t != 13 && __shfl_sync(FULL, nd, t) * (1.0f - 1e-4f) >= round_up_f((T)4 * R2)) continue;
-                const unsigned sbeg = __shfl_sync(FULL, nbeg, t), scnt = __shfl_sync(FULL, ncnt, t);
-                T brx = 0, bry = 0, brz = 0, br2 = (T)INFINITY;
+                if (cbin != 13 && S.nd[cbin] * (1.0f - 1e-4f) >= round_up_f((T)4 * R2)) continue;
+                const unsigned sbeg = S.nbeg[cbin], scnt = S.ncnt[cbin];
+                T drx = 0, dry = 0, drz = 0, dr2 = (T)INFINITY;
                 seedj = 0xFFFFFFFFu;
                 for (unsigned q = lane; q < scnt; q += 32) {
                     const uint32_t j = sbeg + q;
                     T rx, ry, rz, r2;
                     cand(j, rx, ry, rz, r2);
-                    bool keep = (j != self) && r2 > dup2 && r2 < br2;
+                    bool keep = (j != self) && r2 > dup2 && r2 < dr2;
                     if (keep && tgroup >= 0) keep = (int64_t)(P.sgroup ? P.sgroup[j] : 0u) == tgroup;
                     if (keep) {
-                        brx = rx;
-                        bry = ry;
-                        brz = rz;
-                        br2 = r2;
+                        drx = rx;
+                        dry = ry;
+                        drz = rz;
+                        dr2 = r2;
                         seedj = j;
                     }
                 }
-                const bool has = seedj != 0xFFFFFFFFu;
-                const int32_t bcid = has ? (int32_t)(P.sorted[seedj] - pt_base) : 0;
-                status = run_window(has, brx, bry, brz, br2, seedj, bcid);
+                S.sdx[lane] = drx;
+                S.sdy[lane] = dry;
+                S.sdz[lane] = drz;
+                S.sd2[lane] = dr2;
+                S.sdj[lane] = seedj;
+                S.sdcid[lane] = seedj != 0xFFFFFFFFu ? (int32_t)(P.sorted[seedj] - pt_base) : 0;
+                direct = true;
+                seed_step = false;
+            } else {
                 // the bin as lane 0's range (window lane = position mod 32)
-                if (status == ST_OK) status = process(sbeg, lane == 0 ? scnt : 0u, 0u, 0u);
-                seedj = 0xFFFFFFFFu;
-                done |= 1u << t;
+                ba = S.nbeg[S.cbin];
+                ca = lane == 0 ? S.ncnt[S.cbin] : 0u;
+                seed_step = true;
             }
-        }
-    }
-    Ent ea, eb;
-    eb.i = eb.j = eb.k = 0;
-    eb.key = INFINITY;
-    eb.beg = eb.cnt = 0;
-    load_entry(lane, ea);
-    if (kBatch2) load_entry(32 + lane, eb);
-    // lean first pass: a crowded own bin (table entry 0, lane 0's first
-    // entry) sends the cell to the seeded pass
-    if (BASE == kFormLean && P.list_dense && __shfl_sync(FULL, ea.cnt, 0) >= P.seed_min) status = ST_DENSE;
-    while (status == ST_OK) {
-        // The table key is rounded toward zero and the threshold up, so
-        // stopping on key >= thr never drops a bin that could hold a cutter.
-        const float thr = round_up_f((T)4 * R2 * (T)kStopMargin);
-        const bool sa = !(ea.key < thr), sb = kBatch2 && !(eb.key < thr);
-        const unsigned ma = __ballot_sync(FULL, sa), mb = __ballot_sync(FULL, sb);
-        const int na = ma ? __ffs(ma) - 1 : 32;
-        const int nb = (ma || !kBatch2) ? 0 : (mb ? __ffs(mb) - 1 : 32);
-        unsigned ba = ea.beg, ca = lane < na ? ea.cnt : 0u;
-        unsigned bb = eb.beg, cb = lane < nb ? eb.cnt : 0u;
-        // re-test the bins against the current (smaller) radius
-        const float lim4 = round_up_f((T)4 * R2);
-        if (ca && near_ok && near2(ea.i, ea.j, ea.k) * (1.0f - 1e-4f) >= lim4) ca = 0;
-        if (cb && near_ok && near2(eb.i, eb.j, eb.k) * (1.0f - 1e-4f) >= lim4) cb = 0;
-        const bool last = (ma | mb) != 0;
-        const uint32_t used = (uint32_t)(na + nb);
-        t += used;
-        if (kPrefetch && !last) {
-            load_entry(t + lane, ea);
-            if (kBatch2) load_entry(t + 32 + lane, eb);
-        }
-        if constexpr (BASE != kFormLean) ++W.batches;
-        status = process(ba, ca, bb, cb);
-        if (status != ST_OK) break;
-        if (!kPrefetch && !last) {
-            load_entry(t + lane, ea);
-            if (kBatch2) load_entry(t + 32 + lane, eb);
-        }
-        if (last) {
-            phase2 = (t >= tab_len) && isfinite(D.tab_kmax);
+        } else if (ph == 1) {
+            if (!loaded) {
+                load_entry(lane, ea);
+                loaded = true;
+                // lean first pass: a crowded own bin (table entry 0, lane 0's
+                // first entry) sends the cell to the seeded pass
+                if (BASE == kFormLean && P.list_dense && __shfl_sync(FULL, ea.cnt, 0) >= P.seed_min) {
+                    status = ST_DENSE;
+                    break;
+                }
+            }
+            // The table key is rounded toward zero and the threshold up, so
+            // stopping on key >= thr never drops a bin that could hold a cutter.
+            const float thr = round_up_f((T)4 * R2 * (T)kStopMargin);
+            const unsigned ma = __ballot_sync(FULL, !(ea.key < thr));
+            const int na = ma ? __ffs(ma) - 1 : 32;
+            ba = ea.beg;
+            ca = lane < na ? ea.cnt : 0u;
+            // re-test the bins against the current (smaller) radius
+            if (ca && near_ok && near2(ea.i, ea.j, ea.k) * (1.0f - 1e-4f) >= round_up_f((T)4 * R2)) ca = 0;
+            t += (uint32_t)na;
+            if (ma) {
+                ph = (t >= tab_len) && isfinite(D.tab_kmax) ? 2 : 3;
+            } else {
+                load_entry(t + lane, ea);
+            }
+            if constexpr (BASE != kFormLean) ++W.batches;
+        } else if (ph == 2) {
+            const int ring = S.ring;
+            const uint32_t r0 = S.r0;
+            if (r0 == 0) {
+                // a new ring: stop when even its nearest bins are out of reach
+                double lbk = (double)(ring - 1) * D.min_size;
+                lbk = lbk * lbk;
+                if (lbk < D.tab_kmax) lbk = D.tab_kmax;
+                if (ring > cpd - 1 || lbk >= 4.0 * (double)R2 * kStopMargin || (radius >= 0.0 && lbk > radius)) {
+                    ph = 3;
+                    continue;
+                }
+            }
+            const uint32_t rs = 24u * (uint32_t)ring * (uint32_t)ring + 2u;
+            const double thr = 4.0 * (double)R2 * kStopMargin;
+            long long lb = -1;
+            const uint32_t r = r0 + lane;
+            if (r < rs) {
+                int i, j, k;
+                ring_offset(ring, r, i, j, k);
+                const double key = gap_key(D.size, i, j, k);
+                if (key > D.tab_kmax && key < thr && !(radius >= 0.0 && key > radius)) lb = bin_of(i, j, k);
+            }
+            S.r0 = r0 + 32 < rs ? r0 + 32 : 0u;
+            S.ring = r0 + 32 < rs ? ring : ring + 1;
+            if (!__any_sync(FULL, lb >= 0)) continue;
+            if constexpr (BASE != kFormLean) ++W.batches;
+            if (lb >= 0) {
+                ba = P.delims[lb];
+                ca = P.delims[lb + 1] - ba;
+            }
+        } else {
             break;
         }
-    }
-    // phase 2: Chebyshev rings beyond the table (sparse regions)
-    if (status == ST_OK && phase2) {
-        for (int s = 1; s <= cpd - 1 && status == ST_OK; ++s) {
-            double lbk = (double)(s - 1) * D.min_size;
-            lbk = lbk * lbk;
-            if (lbk < D.tab_kmax) lbk = D.tab_kmax;
-            if (lbk >= 4.0 * (double)R2 * kStopMargin) break;
-            if (radius >= 0.0 && lbk > radius) break;
-            const uint32_t rs = 24u * (uint32_t)s * (uint32_t)s + 2u;
-            for (uint32_t r0 = 0; r0 < rs; r0 += 32) {
-                const double thr = 4.0 * (double)R2 * kStopMargin;
-                long long lb = -1;
-                const uint32_t r = r0 + lane;
-                if (r < rs) {
-                    int i, j, k;
-                    ring_offset(s, r, i, j, k);
-                    const double key = gap_key(D.size, i, j, k);
-                    if (key > D.tab_kmax && key < thr && !(radius >= 0.0 && key > radius)) lb = bin_of(i, j, k);
-                }
-                if (!__any_sync(FULL, lb >= 0)) continue;
-                if constexpr (BASE != kFormLean) ++W.batches;
-                unsigned beg = 0, cnt = 0;
-                if (lb >= 0) {
-                    beg = P.delims[lb];
-                    cnt = P.delims[lb + 1] - beg;
-                }
-                status = process(beg, cnt, 0u, 0u);
-                if (status != ST_OK) break;
-            }
+        status = process(ba, ca, direct);
+        if (kSeedForm && ph == 0 && seed_step) {
+            // a crowded bin's windows are done
+            seedj = 0xFFFFFFFFu;
+            done |= 1u << S.cbin;
         }
     }
 
