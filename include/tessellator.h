@@ -104,7 +104,7 @@ typedef struct {
     void* stream;
     uint32_t flags;
     /* A cell whose own bin holds at least this many points first cuts by the
-     * nearest point of each lane's stride of that bin (crowded bins); 0: 48.
+     * nearest point of each lane's stride of that bin (crowded bins); 0: 12.
      * A launch knob only: results do not depend on it. */
     int32_t crowded_bin;
 } tess_config;
@@ -138,7 +138,7 @@ typedef struct {
     /* FP32 form: of the rerun_fp64 cells, those the hybrid re-run (guard-band
      * tests decided in FP64) could not settle, re-run entirely in FP64 */
     uint64_t rerun_fp64_full;
-    /* FP32 form: cells whose own bin is crowded (>= 48 points), taken out of
+    /* FP32 form: cells whose own bin is crowded (>= crowded_bin points), taken out of
      * the first pass and computed by a pass that first cuts by the nearest
      * point of each lane's stride of that bin */
     uint64_t dense_cells;
@@ -364,7 +364,7 @@ typedef struct {
     int32_t trials;            /* candidate knob sets timed (0: read from the cache) */
     int32_t from_cache;        /* 1: the choice came from the cache file             */
     uint32_t max_bin_points;   /* the input's most crowded bin (points)             */
-    double crowded_fraction;   /* share of points in bins of >= 48 points           */
+    double crowded_fraction;   /* share of points in bins of >= 12 points           */
 } tess_tuning;
 
 /* Tune d's knobs for `precision`.  The choice is kept by the handle for every

@@ -11,7 +11,7 @@ from oracle import report
 pytestmark = pytest.mark.gpu
 
 WPB = {4, 8}
-CROWD = {32, 48, 96, 192}
+CROWD = {8, 12, 24, 48}
 DENSITY = {0.6, 1.25, 2.5}
 
 

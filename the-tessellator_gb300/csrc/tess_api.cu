@@ -277,7 +277,9 @@ struct Engine {
     }
 };
 
-constexpr int32_t kDefaultCrowdedBin = 48;
+// Measured on the clustered 4M set (first pass + re-runs): 257.9 ms at 48,
+// 238.7 ms at 24, 231.2 ms at 12; uniform inputs have no bin that large.
+constexpr int32_t kDefaultCrowdedBin = 12;
 
 void fill_defaults(tess_config* c) {
     c->guard_rel = 4e-7;
@@ -872,7 +874,7 @@ tess_status time_sample(Engine& E, int precision, uint32_t m, float* ms) {
 // density by timing each candidate on an evenly spaced sample of up to
 // 262,144 cells in bin order (the whole box, every diagram), two runs each,
 // the faster counted.  Candidates: warps per block {4, 8} (the clipping
-// kernel's launch bound allows 8 at most), crowded bin {32, 48, 96, 192},
+// kernel's launch bound allows 8 at most), crowded bin {12, 8, 24, 48},
 // density {0.6, 1.25, 2.5} points per bin (batches).
 tess_status engine_autotune(Engine& E, int precision, bool batch, const char* cache_path, tess_tuning* out) {
     if (!E.built) return fail(TESS_E_STATE, "the grid is not built");
@@ -929,7 +931,7 @@ tess_status engine_autotune(Engine& E, int precision, bool batch, const char* ca
     T.sample_cells = m;
     std::vector<double> dens = batch ? std::vector<double>{1.25, 0.6, 2.5} : std::vector<double>{E.cfg.bin_density};
     const int wpbs[] = {8, 4};
-    const int crowds[] = {48, 32, 96, 192};
+    const int crowds[] = {12, 8, 24, 48};
     float best = INFINITY;
     int bw = 8, bc = kDefaultCrowdedBin;
     double bd = dens[0];

@@ -66,7 +66,7 @@ constexpr bool kPrefetch = true;
 // first-pass form leaves it out: on uniform inputs windows are small and its
 // mere presence costs the hot loop registers.
 constexpr int kPretestMin = 2;
-// A site whose own bin holds at least ClipParams::seed_min points (48 by
+// A site whose own bin holds at least ClipParams::seed_min points (12 by
 // default, autotuned per input) is seeded before the shell walk: every lane
 // takes the nearest point of its stride of that bin and the 32 seeds are cut
 // nearest first.  In crowded bins the walk's 32-point windows otherwise meet
