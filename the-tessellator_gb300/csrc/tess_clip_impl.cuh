@@ -98,7 +98,6 @@ struct Smem {
             T pn[P];                          // |normal| (1 for the FP64 form and the walls)
             T vsd[V];                         // signed distances of the current cut
             T vr[V];                          // (|v| + e_v)^2 of each slot (FP32), |v|^2 (FP64)
-            uint32_t cpref[32], cbeg[32];     // candidate batch: prefix counts, bin starts
             uint32_t nbeg[32], ncnt[32];      // crowded bins: the 27 neighbour bins' ranges ...
             float nd[32];                     // ... and the squared distance to their nearest point
             uint32_t pending;                 // crowded bins still to handle (mask over the 27)
@@ -1184,13 +1183,11 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     // [beg, beg + cnt), in lane order; or (direct) by one window of the
     // lanes' seeds of a crowded bin (S.sd*).
     auto process = [&](unsigned beg, unsigned cnt, bool direct) -> int {
-        unsigned total = 32;
+        unsigned total = 32, pref = 0;
         if (!direct) {
             const unsigned inc = warp_incl_scan_u(cnt, lane);
             total = __shfl_sync(FULL, inc, 31);
-            S.cpref[lane] = inc - cnt;
-            S.cbeg[lane] = beg;
-            __syncwarp();
+            pref = inc - cnt;
         }
         for (unsigned w0 = 0; w0 < total; w0 += 32) {
             bool keep = false;
@@ -1210,14 +1207,14 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 if constexpr (BASE != kFormLean) ++W.windows;
                 const unsigned c = w0 + lane;
                 const T lim = (T)4 * R2 * (T)kStopMargin;
+                // the lane's bin: the last with prefix <= c (never an empty one)
+                int lo = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(FULL, pref, lo + step) <= c) lo += step;
+                const unsigned bbeg = __shfl_sync(FULL, beg, lo), bpref = __shfl_sync(FULL, pref, lo);
                 if (c < total) {
-                    int lo = 0, hi = 31;
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (S.cpref[mid] <= c) lo = mid;
-                        else hi = mid - 1;
-                    }
-                    j = S.cbeg[lo] + (c - S.cpref[lo]);
+                    j = bbeg + (c - bpref);
                     cand(j, rx, ry, rz, r2);
                     keep = (j != self) && r2 > dup2 && r2 < lim;
                     if constexpr (GUARD) near = (j != self) && !(r2 > dup2);
