@@ -43,7 +43,8 @@ typedef enum {
     TESS_E_OVERFLOW = 4,  /* a cell exceeded the largest vertex/face capacity          */
     TESS_E_STATE = 5,     /* results requested before tess_diagram_compute_all         */
     TESS_E_NOMEM = 6,     /* device or host allocation failed                          */
-    TESS_E_LIMIT = 7      /* an iteration cap or wait limit was reached                */
+    TESS_E_LIMIT = 7,     /* an iteration cap or wait limit was reached                */
+    TESS_E_CHECK = 8      /* checked build only: a device index was out of range        */
 } tess_status;
 
 typedef enum {

@@ -16,6 +16,7 @@ pub const TESS_E_OVERFLOW: tess_status = 4;  // a cell exceeded the largest capa
 pub const TESS_E_STATE: tess_status = 5;     // results asked for before compute
 pub const TESS_E_NOMEM: tess_status = 6;
 pub const TESS_E_LIMIT: tess_status = 7;
+pub const TESS_E_CHECK: tess_status = 8;
 pub const TESS_PRECISION_FP64: c_int = 0;
 pub const TESS_PRECISION_FP32_GUARD: c_int = 1;
 pub const TESS_PRECISION_MIXED: c_int = 2;   // FP32 clipping, FP64-accurate results

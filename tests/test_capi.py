@@ -174,3 +174,30 @@ def test_struct_layouts_agree(tess, cname, pyname):
     body = re.search(r"pub struct " + cname + r" \{(.*?)\}", text, flags=re.S).group(1)
     assert re.findall(r"pub (\w+):", body) == fields
 
+
+
+def test_checked_build_loads_and_matches_the_exports():
+    """The bounds-checked build (TESS_CHECKED=1) exports the same functions as
+    the library, loads without a GPU and fails loudly there like it."""
+    import ctypes
+
+    import build_lib
+
+    lib = build_lib.build(checked=True)
+    syms = exported_symbols(lib)
+    missing = [f for f in declared_functions() if f not in syms]
+    assert not missing, missing
+    assert {x for x in syms if x.startswith("tess_")} == \
+        {x for x in exported_symbols(build_lib.build()) if x.startswith("tess_")}
+    chk = ctypes.CDLL(lib)
+    cfg = (ctypes.c_char * 4096)()
+    chk.tess_config_default(cfg)
+    pytest.importorskip("torch")
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    pts = (ctypes.c_double * 30)(*([0.1] * 30))
+    h = ctypes.c_void_p()
+    st = chk.tess_diagram_create(pts, ctypes.c_size_t(10), None, None, None, cfg, ctypes.byref(h))
+    assert st == 2   # TESS_E_CUDA

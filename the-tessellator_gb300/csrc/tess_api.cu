@@ -152,6 +152,7 @@ struct Engine {
     uint32_t* d_sgroup = nullptr;
     TabEntry* d_table = nullptr;
     int* d_err = nullptr;
+    int* d_check = nullptr;     // checked build: out-of-range index sites (CheckSite bits)
     // results
     double* d_vol = nullptr;
     uint32_t* d_nface = nullptr;
@@ -243,7 +244,7 @@ struct Engine {
         dfree(d_xyz); dfree(d_groups); dfree(d_desc); dfree(d_chunk_diag); dfree(d_chunk_start);
         dfree(d_bounds); dfree(d_bin); dfree(d_rank); dfree(d_delims); dfree(d_scan_tmp);
         dfree(d_sorted); dfree(d_inv); dfree(d_spx); dfree(d_spy); dfree(d_spz); dfree(d_shi); dfree(d_slo); dfree(d_sgroup);
-        dfree(d_table); dfree(d_err); dfree(d_vol); dfree(d_nface); dfree(d_fstart); dfree(d_status);
+        dfree(d_table); dfree(d_err); dfree(d_check); dfree(d_vol); dfree(d_nface); dfree(d_fstart); dfree(d_status);
         dfree(d_fnbr); dfree(d_farea); dfree(d_fcursor);
         for (auto& l : d_list) dfree(l);
         dfree(d_counters); dfree(d_work); dfree(d_offs); dfree(d_cnbr); dfree(d_carea); dfree(d_csr_tmp);
@@ -411,6 +412,8 @@ tess_status engine_init(Engine& E, const tess_config* cfg, std::vector<DiagDesc>
     TRY(dalloc(&E.d_table, E.table_total));
     E.table_alloc = E.table_total;
     TRY(dalloc(&E.d_err, 1));
+    TRY(dalloc(&E.d_check, 1));
+    CU(cudaMemsetAsync(E.d_check, 0, sizeof(int), E.stream));
     TRY(dalloc(&E.d_vol, n));
     TRY(dalloc(&E.d_nface, n));
     TRY(dalloc(&E.d_fstart, n));
@@ -456,7 +459,26 @@ GridBuffers grid_buffers(Engine& E) {
     g.table = E.d_table;
     g.table_gaps = E.cfg.table_gaps;
     g.error_flag = E.d_err;
+    g.check = E.d_check;
     return g;
+}
+
+// The checked build's verdict on the launches so far: TESS_E_CHECK once any
+// device index was out of range (the word stays set for the handle).  The
+// regular build reads nothing.
+tess_status check_word(Engine& E) {
+#if TESS_CHECKED
+    int w = 0;
+    CU(cudaMemcpyAsync(&w, E.d_check, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
+    CU(cudaStreamSynchronize(E.stream));
+    if (w)
+        return fail(TESS_E_CHECK,
+                    "checked build: out-of-range device index (sites 0x%x: 1 point, 2 bin, 4 slot, 8 plane, 16 list, "
+                    "32 face, 64 sort)", w);
+#else
+    (void)E;
+#endif
+    return TESS_OK;
 }
 
 tess_status engine_build(Engine& E, bool check) {
@@ -488,6 +510,7 @@ tess_status engine_build(Engine& E, bool check) {
         CU(cudaEventSynchronize(ev.e[1]));
         E.stats.ms_grid = ev.ms(0, 1);
     }
+    TRY(check_word(E));
     E.built = true;
     E.computed = false;
     E.csr_valid = false;
@@ -524,6 +547,9 @@ ClipParams base_params(Engine& E) {
     p.guard_rel = (float)E.cfg.guard_rel;
     p.verify_rel = (float)E.cfg.verify_rel;
     p.grid_err = E.d_err;
+    p.check = E.d_check;
+    p.npts = E.total;
+    p.nbins = E.total_bins;
     p.seed_min = (uint32_t)(E.cfg.crowded_bin > 0 ? E.cfg.crowded_bin : kDefaultCrowdedBin);
     return p;
 }
@@ -696,6 +722,7 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
         E.stats.rerun_guard = counts[L_REASON + ST_GUARD];
         E.stats.rerun_verify = counts[L_REASON + ST_VERIFY];
         E.stats.rerun_degenerate = counts[L_REASON + ST_DEGEN];
+        TRY(check_word(E));
         if (failed) return fail(TESS_E_OVERFLOW, "%llu cells could not be computed", (unsigned long long)failed);
         return TESS_OK;
     }
@@ -1014,6 +1041,7 @@ tess_status engine_geo(Engine& E, int precision, uint32_t gs, const double* poin
         CU(launch_clip(p, prec == TESS_PRECISION_FP32_GUARD ? 1 : 0, 8, kFormStd, 1, 1, E.stream));
         CU(cudaMemcpyAsync(out, E.d_geo, sizeof(GeoOut), cudaMemcpyDeviceToHost, E.stream));
         CU(cudaStreamSynchronize(E.stream));
+        TRY(check_word(E));
         if (out->status == ST_OK) return TESS_OK;
         if (prec == TESS_PRECISION_FP64) break;
     }
@@ -1675,6 +1703,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
     CU(cudaMemcpyAsync(counts, E.d_counters + 16, sizeof(counts), cudaMemcpyDeviceToHost, E.stream));
     CU(cudaMemcpyAsync(&gerr, E.d_err, sizeof(int), cudaMemcpyDeviceToHost, E.stream));
     CU(cudaStreamSynchronize(E.stream));
+    TRY(check_word(E));
     if (timing) E.stats.ms_clip = ev.ms(0, 1);
     if (gerr == 1) {
         E.computed = false;

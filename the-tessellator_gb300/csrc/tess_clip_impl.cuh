@@ -359,7 +359,7 @@ struct Regs {
 template <typename T, int K, bool GUARD, bool RESOLVE>
 __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, const Regs<T, K> sdv,
                                         const Regs<uint32_t, K> omv, T nx, T ny, T nz, T off, T rn, T cR,
-                                        T gr, int32_t id, uint32_t src, int f, int lane) {
+                                        T gr, int32_t id, uint32_t src, int f, int lane, int* P_check) {
     using S_t = Smem<T, K>;
     const T(&sd)[K] = sdv.v;
     const uint32_t(&om)[K] = omv.v;
@@ -440,7 +440,8 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
         for (int k = 0; k < K; ++k)
 #pragma unroll
             for (int e = 0; e < 3; ++e)
-                if (bnd & (1u << (3 * k + e))) items[qq++] = (uint16_t)((k * 32 + lane) | (e << 8));
+                if (bnd & (1u << (3 * k + e)))
+                    items[tess_chk(qq++, S_t::V + 32, P_check, CK_SLOT)] = (uint16_t)((k * 32 + lane) | (e << 8));
     }
     __syncwarp();
     uint32_t newm[K];
@@ -498,7 +499,7 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
                 py = xy + (yy - xy) * t;
                 pz = xz + (yz - xz) * t;
             }
-            slot = select_k<K>(fm, qi);
+            slot = tess_chk(select_k<K>(fm, qi), S_t::V, P_check, CK_SLOT);
         }
         if (RESOLVE && __any_sync(FULL, numbad)) return -ST_GUARD;
         __syncwarp();
@@ -635,7 +636,7 @@ __device__ __noinline__ int resolve_fp64(const Smem<T, K>& S, const ClipParams& 
             n[e][2] = a == 2 ? (mx ? 1.0 : -1.0) : 0.0;
             h[e] = mx ? (st.bhi[a] - s_a) : (s_a - st.blo[a]);
         } else {
-            const uint32_t j = S.psrc[p];
+            const uint32_t j = tess_chk(S.psrc[p], P.npts, P.check, CK_POINT);
             n[e][0] = P.spx[j] - st.sx;
             n[e][1] = P.spy[j] - st.sy;
             n[e][2] = P.spz[j] - st.sz;
@@ -653,6 +654,7 @@ __device__ __noinline__ int resolve_fp64(const Smem<T, K>& S, const ClipParams& 
     const double x = (h[0] * bc0 + h[1] * ca0 + h[2] * ab0) / det;
     const double y = (h[0] * bc1 + h[1] * ca1 + h[2] * ab1) / det;
     const double z = (h[0] * bc2 + h[1] * ca2 + h[2] * ab2) / det;
+    cj = tess_chk(cj, P.npts, P.check, CK_POINT);
     const double qx = P.spx[cj] - st.sx, qy = P.spy[cj] - st.sy, qz = P.spz[cj] - st.sz;
     const double q2 = qx * qx + qy * qy + qz * qz;
     const double sd = (qx * x + qy * y + qz * z - 0.5 * q2) / sqrt(q2);
@@ -745,7 +747,8 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         for (int k = 0; k < K; ++k) {
             const int s = k * 32 + lane;
             if (!GUARD && ((C.lm[k] >> lane) & 1u)) S.vsd[s] = sd[k];   // read by the FP64 interpolation
-            if ((om[k] >> lane) & 1u) S.fl[base + before + __popc(om[k] & ((1u << lane) - 1u))] = (uint8_t)s;
+            if ((om[k] >> lane) & 1u)
+                S.fl[tess_chk(base + before + __popc(om[k] & ((1u << lane) - 1u)), S_t::V + 32, P.check, CK_SLOT)] = (uint8_t)s;
             before += __popc(om[k]);
         }
         __syncwarp();
@@ -755,7 +758,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         if (edge) {
             const int xi = (lane * 11) >> 5;          // lane / 3 for lane < 32
             const int e = lane - 3 * xi;
-            x = S.fl[base + xi];
+            x = tess_chk((int)S.fl[tess_chk(base + xi, S_t::V + 32, P.check, CK_SLOT)], S_t::V, P.check, CK_SLOT);
             const uint32_t xt_ = S.tri[x], xa_ = S.adj[x];
             a = plane_of(xt_, e);
             b = plane_of(xt_, e == 2 ? 0 : e + 1);
@@ -805,7 +808,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
                 pz = xz + (yz - xz) * t;
             }
             ty = S.tri[y];
-            slot = S.fl[base + R - 1 - q];
+            slot = tess_chk((int)S.fl[tess_chk(base + R - 1 - q, S_t::V + 32, P.check, CK_SLOT)], S_t::V, P.check, CK_SLOT);
         }
         if (RESOLVE && __any_sync(FULL, numbad)) return -ST_GUARD;
         __syncwarp();
@@ -871,7 +874,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         sdv.v[k] = sd[k];
         omv.v[k] = om[k];
     }
-    return cut_general<T, K, GUARD, RESOLVE>(S, C, sdv, omv, nx, ny, nz, off, rn, cR, gr, id, src, f, lane);
+    return cut_general<T, K, GUARD, RESOLVE>(S, C, sdv, omv, nx, ny, nz, off, rn, cR, gr, id, src, f, lane, P.check);
 }
 
 // Squared radius of the cell about its site: max |v|^2 over live vertices;
@@ -953,7 +956,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         sy = P.spy[gs];
         sz = P.spz[gs];
         self = gs;
-        orig = P.sorted[gs];
+        orig = tess_chk(P.sorted[tess_chk(gs, P.npts, P.check, CK_POINT)], P.npts, P.check, CK_POINT);
     }
     // FP32 form: the site as an FP32 pair (hi + lo) relative to the diagram's
     // centre, like the points, so candidate offsets (p - site) come out of
@@ -1214,7 +1217,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     if (__shfl_sync(FULL, pref, lo + step) <= c) lo += step;
                 const unsigned bbeg = __shfl_sync(FULL, beg, lo), bpref = __shfl_sync(FULL, pref, lo);
                 if (c < total) {
-                    j = bbeg + (c - bpref);
+                    j = tess_chk(bbeg + (c - bpref), P.npts, P.check, CK_POINT);
                     cand(j, rx, ry, rz, r2);
                     keep = (j != self) && r2 > dup2 && r2 < lim;
                     if constexpr (GUARD) near = (j != self) && !(r2 > dup2);
@@ -1268,7 +1271,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         // no point of this bin can cut: it lies beyond twice the cell radius
         if (near_ok && near2(i, j, k) * (1.0f - 1e-4f) >= round_up_f((T)4 * R2))
             return -1;
-        return (long long)(bin_base + ((uint64_t)x * cpd + y) * cpd + z);
+        return (long long)tess_chk(bin_base + ((uint64_t)x * cpd + y) * cpd + z, P.nbins, P.check, CK_BIN);
     };
 
     // Phases of the walk:
@@ -1384,7 +1387,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     // would stay live through every later cut)
     bool seed_step = true;       // phase 0: the next step cuts a bin's seeds
     if constexpr (kSeedForm) {
-        const uint64_t sb = bin_base + ((uint64_t)cbx * cpd + cby) * cpd + cbz;
+        const uint64_t sb = tess_chk(bin_base + ((uint64_t)cbx * cpd + cby) * cpd + cbz, P.nbins, P.check, CK_BIN);
         if (P.delims[sb + 1] - P.delims[sb] >= P.seed_min) {
             const int ti = lane / 9 - 1, tj = (lane / 3) % 3 - 1, tk = lane % 3 - 1;
             unsigned nb = 0, nc = 0;
@@ -1429,7 +1432,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 T drx = 0, dry = 0, drz = 0, dr2 = (T)INFINITY;
                 seedj = 0xFFFFFFFFu;
                 for (unsigned q = lane; q < scnt; q += 32) {
-                    const uint32_t j = sbeg + q;
+                    const uint32_t j = tess_chk(sbeg + q, P.npts, P.check, CK_POINT);
                     T rx, ry, rz, r2;
                     cand(j, rx, ry, rz, r2);
                     bool keep = (j != self) && r2 > dup2 && r2 < dr2;
@@ -1585,7 +1588,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     q2 = a == 2 ? (mx ? 1.f : -1.f) : 0.f;
                     dist = hh;
                 } else {
-                    const uint32_t j = S.psrc[p];
+                    const uint32_t j = tess_chk(S.psrc[p], P.npts, P.check, CK_POINT);
                     float sh, se;
                     two_sum(P.shi[3ull * j], -shx, sh, se);
                     two_sum(sh, (P.slo[3ull * j] - slx) + se, q0, l0);
@@ -1636,7 +1639,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     qz = a == 2 ? (mx ? 1.0 : -1.0) : 0.0;
                     dist = (float)qh;
                 } else {
-                    const uint32_t j = S.psrc[p];
+                    const uint32_t j = tess_chk(S.psrc[p], P.npts, P.check, CK_POINT);
                     qx = P.spx[j] - sx;
                     qy = P.spy[j] - sy;
                     qz = P.spz[j] - sz;
@@ -1734,7 +1737,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             farea[r] = 0.0;
             fdegr[r] = 0;
             if (p < C.np && S.fdeg[p] > 0) {
-                const int start = S.fsta[p];
+                const int start = tess_chk((int)S.fsta[p], S_t::V, P.check, CK_SLOT);
                 int cur = start, steps = 0;
                 if constexpr (EXACT) {
                     // The face's area from its projection on the plane normal
@@ -1860,7 +1863,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 count = P.list_dense_count;
             }
             if (list) {
-                list[atomicAdd(count, 1u)] = gs;
+                list[tess_chk(atomicAdd(count, 1u), P.npts, P.check, CK_LIST)] = gs;
                 P.status[orig] = ST_PENDING;
             } else {
                 P.status[orig] = (uint8_t)status;
@@ -1923,7 +1926,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 const int p = S.rank2p[q];
                 G->face_off[q] = off;
                 const int deg = (int)S.fdeg[p];
-                const int start = S.fsta[p];
+                const int start = tess_chk((int)S.fsta[p], S_t::V, P.check, CK_SLOT);
                 int cur = start;
                 // reversed walk: counter-clockwise seen from outside
                 for (int st = 0; st < deg; ++st) {
@@ -1932,7 +1935,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                         if ((cur >> 5) == k) vi += __popc(C.lm[k] & ((1u << (cur & 31)) - 1u));
                         else if ((cur >> 5) > k) vi += __popc(C.lm[k]);
                     }
-                    G->face_vtx[off + (deg - st) % deg] = vi;
+                    G->face_vtx[tess_chk(off + (deg - st) % deg, 3 * 256, P.check, CK_FACE)] = vi;
                     const uint32_t tt = S.tri[cur], aa = S.adj[cur];
                     const int i = plane_of(tt, 0) == p ? 0 : (plane_of(tt, 1) == p ? 1 : 2);
                     cur = plane_of(aa, i) % S_t::V;
@@ -1960,8 +1963,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         if (fdegr[r] > 0) {
-            P.face_nbr[fbase + rank[r]] = S.pid[r * 32 + lane];
-            P.face_area[fbase + rank[r]] = farea[r];
+            const unsigned long long fi = tess_chk(fbase + rank[r], P.face_cap, P.check, CK_FACE);
+            P.face_nbr[fi] = S.pid[r * 32 + lane];
+            P.face_area[fi] = farea[r];
         }
     }
     if (lane == 0) {

@@ -195,7 +195,7 @@ __global__ void k_bin_count(GridBuffers g) {
             if (!oky) by = axis_index(y, D.glo[1], D.ghi[1], D.inv[1], cpd);
             if (!okz) bz = axis_index(z, D.glo[2], D.ghi[2], D.inv[2], cpd);
             // get_cell_from_indices, celery.rs:317-325
-            const uint64_t b = D.bin_base + ((uint64_t)bx * cpd + by) * cpd + bz;
+            const uint64_t b = tess_chk(D.bin_base + ((uint64_t)bx * cpd + by) * cpd + bz, g.total_bins, g.check, CK_GRID);
             g.bin[i] = (uint32_t)b;
             g.rank[i] = atomicAdd(&g.delims[b], 1u);
         }
@@ -276,7 +276,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(uint32_t* data, uin
 __global__ void k_scatter(GridBuffers g) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.total) return;
-    g.sorted[g.delims[g.bin[i]] + g.rank[i]] = i;
+    const uint32_t b = tess_chk(g.bin[i], g.total_bins, g.check, CK_GRID);
+    g.sorted[tess_chk(g.delims[b] + g.rank[i], g.total, g.check, CK_GRID)] = i;
 }
 
 // Ascending sort of a[0, n) by one block: a bitonic network in the form whose
@@ -407,7 +408,7 @@ __device__ __forceinline__ bool split_rn_int(double u, float& hi, float& lo) {
 __global__ void k_gather(GridBuffers g) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.total) return;
-    const uint32_t i = g.sorted[s];
+    const uint32_t i = tess_chk(g.sorted[s], g.total, g.check, CK_GRID);
     g.inv[i] = s;
     const double x = g.xyz[3ull * i], y = g.xyz[3ull * i + 1], z = g.xyz[3ull * i + 2];
     g.spx[s] = x;

@@ -37,6 +37,38 @@ enum CellStatus : uint8_t {
     ST_PENDING = 255    // not computed yet
 };
 
+// The checked build (compiled with TESS_CHECKED=1, libtessgpu_checked.so): the
+// binning and clipping kernels test every data-dependent index into a device
+// array before use.  An index outside [0, n) sets bit `site` of the handle's
+// check word and is replaced by 0, so the access stays in bounds; the host
+// then fails the call with TESS_E_CHECK.  The regular build compiles no test.
+#ifndef TESS_CHECKED
+#define TESS_CHECKED 0
+#endif
+enum CheckSite : int {
+    CK_POINT = 0,   // a point (sorted or original index)
+    CK_BIN = 1,     // a bin of the grid
+    CK_SLOT = 2,    // a vertex slot or free-slot stack entry of a cell
+    CK_PLANE = 3,   // a plane of a cell
+    CK_LIST = 4,    // an entry of a re-run list
+    CK_FACE = 5,    // a face of the face pool
+    CK_GRID = 6     // a position of the binning pass's sort
+};
+template <typename I, typename N>
+__device__ __forceinline__ I tess_chk(I i, N n, int* check, int site) {
+#if TESS_CHECKED
+    if (!((unsigned long long)(long long)i < (unsigned long long)n)) {
+        if (check) atomicOr(check, 1 << site);
+        return (I)0;
+    }
+#else
+    (void)n;
+    (void)check;
+    (void)site;
+#endif
+    return i;
+}
+
 // One diagram as the kernels see it.  Filled partly by the host (counts,
 // bases, box) and partly on the device (bounds, bin sizes, table length).
 struct DiagDesc {
@@ -150,6 +182,7 @@ struct GridBuffers {
     TabEntry* table;
     int table_gaps;
     int* error_flag;            // set when an input coordinate is not finite
+    int* check;                 // checked build: the check word
 };
 constexpr uint32_t kChunk = 8192;
 constexpr int kScanItems = 8;       // items per thread in the scan
@@ -290,6 +323,10 @@ struct ClipParams {
     // the clipping kernels return at once (the batch graph runs every pass
     // without a host check in between)
     const int* grid_err;
+    // checked build: the check word, the points and the bins of the set
+    int* check;
+    uint32_t npts;
+    uint64_t nbins;
 };
 
 // Forms of the clipping kernel:

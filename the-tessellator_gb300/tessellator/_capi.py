@@ -12,9 +12,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libtessgpu.so")
 
 TESS_OK, TESS_E_INVALID, TESS_E_CUDA, TESS_E_CAPACITY = 0, 1, 2, 3
-TESS_E_OVERFLOW, TESS_E_STATE, TESS_E_NOMEM, TESS_E_LIMIT = 4, 5, 6, 7
+TESS_E_OVERFLOW, TESS_E_STATE, TESS_E_NOMEM, TESS_E_LIMIT, TESS_E_CHECK = 4, 5, 6, 7, 8
 STATUS_NAMES = {0: "TESS_OK", 1: "TESS_E_INVALID", 2: "TESS_E_CUDA", 3: "TESS_E_CAPACITY",
-                4: "TESS_E_OVERFLOW", 5: "TESS_E_STATE", 6: "TESS_E_NOMEM", 7: "TESS_E_LIMIT"}
+                4: "TESS_E_OVERFLOW", 5: "TESS_E_STATE", 6: "TESS_E_NOMEM", 7: "TESS_E_LIMIT",
+                8: "TESS_E_CHECK"}
 PRECISION_FP64, PRECISION_FP32_GUARD, PRECISION_MIXED = 0, 1, 2
 FLAG_TIMING = 1
 FLAG_COUNTERS = 2
