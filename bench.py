@@ -57,9 +57,9 @@ NCU_CLIP_BYTES_PER_CELL = 14.724912e9 * 16.963904e-3 / 1_000_000
 # kernel is bound by instruction issue, so this gives its issue roofline.
 NCU_CLIP_INST_PER_CELL = 13_255_807_231 / 1_000_000
 NCU_RADIUS_BYTES = {"count": 3.846207488e9 + 0.50285184e9, "fill": 6.337812736e9 + 1.53743616e9}
-# DRAM traffic of the 11 binning launches (read 709.1 MB + write 217.2 MB) at
+# DRAM traffic of the 11 binning launches (read 651.8 MB + write 183.7 MB) at
 # 4,194,304 uniform points, scaled by points: every term is per point or per bin.
-NCU_GRID_BYTES_PER_POINT = (709.1e6 + 217.2e6) / 4_194_304
+NCU_GRID_BYTES_PER_POINT = (651.8e6 + 183.7e6) / 4_194_304
 
 
 def l2_note(input_bytes, written_bytes):

@@ -153,6 +153,7 @@ struct Engine {
     TabEntry* d_table = nullptr;
     int* d_err = nullptr;
     int* d_check = nullptr;     // checked build: out-of-range index sites (CheckSite bits)
+    bool inv_valid = false;     // d_inv matches the current binning
     // results
     double* d_vol = nullptr;
     uint32_t* d_nface = nullptr;
@@ -449,7 +450,7 @@ GridBuffers grid_buffers(Engine& E) {
     g.delims = E.d_delims;
     g.scan_tmp = E.d_scan_tmp;
     g.sorted = E.d_sorted;
-    g.inv = E.d_inv;
+    g.inv = nullptr;   // built on demand (ensure_inv)
     g.spx = E.d_spx;
     g.spy = E.d_spy;
     g.spz = E.d_spz;
@@ -461,6 +462,18 @@ GridBuffers grid_buffers(Engine& E) {
     g.error_flag = E.d_err;
     g.check = E.d_check;
     return g;
+}
+
+// The point -> sorted position map, built on first use after a binning pass.
+tess_status ensure_inv(Engine& E) {
+    if (E.inv_valid) return TESS_OK;
+    CU(launch_inverse(E.d_sorted, E.d_inv, E.total, E.d_check, E.stream));
+    // the handle's stream does not block with the legacy default stream:
+    // finish here, so plain copies of single entries see the map
+    CU(cudaStreamSynchronize(E.stream));
+    E.launches += 1;
+    E.inv_valid = true;
+    return TESS_OK;
 }
 
 // The checked build's verdict on the launches so far: TESS_E_CHECK once any
@@ -512,6 +525,7 @@ tess_status engine_build(Engine& E, bool check) {
     }
     TRY(check_word(E));
     E.built = true;
+    E.inv_valid = false;
     E.computed = false;
     E.csr_valid = false;
     E.rtab_valid = false;
@@ -1079,6 +1093,7 @@ tess_status engine_radius(Engine& E, int mode, bool by_cell, const double* qxyz,
     p.spz = E.d_spz;
     p.sgroup = E.d_sgroup;
     p.xyz = E.d_xyz;
+    TRY(ensure_inv(E));
     p.inv = E.d_inv;
     p.nq = (uint32_t)nq;
     p.radius = radius;
@@ -1459,6 +1474,7 @@ static tess_status geo_for(tess_diagram* d, size_t i, GeoOut* g) {
     TRY(cell_check(d, i));
     uint32_t gs = 0;
     CU(cudaSetDevice(d->E.device));
+    TRY(ensure_inv(d->E));
     CU(cudaMemcpy(&gs, d->E.d_inv + i, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     return engine_geo(d->E, d->E.last_precision, gs, nullptr, d->E.last_radius, d->E.last_group, nullptr, nullptr, g);
 }
@@ -1522,6 +1538,7 @@ static tess_status single_cell(tess_diagram* d, const size_t* i, const double* p
     CU(cudaSetDevice(d->E.device));
     if (i) {
         if (*i >= d->n) return fail(TESS_E_INVALID, "cell index %zu out of range (n = %u)", *i, d->n);
+        TRY(ensure_inv(d->E));
         CU(cudaMemcpy(&gs, d->E.d_inv + *i, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     } else if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[2])) {
         return fail(TESS_E_INVALID, "point must be finite");

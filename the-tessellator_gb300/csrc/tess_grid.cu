@@ -409,7 +409,7 @@ __global__ void k_gather(GridBuffers g) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.total) return;
     const uint32_t i = tess_chk(g.sorted[s], g.total, g.check, CK_GRID);
-    g.inv[i] = s;
+    if (g.inv) g.inv[i] = s;
     const double x = g.xyz[3ull * i], y = g.xyz[3ull * i + 1], z = g.xyz[3ull * i + 2];
     g.spx[s] = x;
     g.spy[s] = y;
@@ -438,6 +438,15 @@ __global__ void k_gather(GridBuffers g) {
 // One block per diagram: every offset within Chebyshev radius `cheb` whose key
 // is <= tab_kmax, sorted by (key, i, j, k) with a bitonic sort in shared memory.
 constexpr int kTabThreads = 1024;
+
+// The inverse permutation, point -> sorted position, for the queries that
+// start from a point's original index (radius queries by cell, single-cell
+// computes).  Built on first use after a binning pass rather than in it: its
+// 4-byte scatter writes cost a partial DRAM sector per point.
+__global__ void k_inverse(const uint32_t* sorted, uint32_t* inv, uint32_t n, int* check) {
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+        inv[tess_chk(sorted[s], n, check, CK_GRID)] = s;
+}
 
 __global__ void __launch_bounds__(kTabThreads) k_table(GridBuffers g) {
     __shared__ unsigned long long skey[kMaxTable];
@@ -542,6 +551,12 @@ __global__ void k_bounds_init(unsigned long long* b, int ndiag) {
     if (t < 6 * ndiag) b[t] = (t % 6) < 3 ? ~0ull : 0ull;
 }
 }  // namespace
+
+cudaError_t launch_inverse(const uint32_t* sorted, uint32_t* inv, uint32_t n, int* check, cudaStream_t s) {
+    const uint32_t blocks = std::min<uint32_t>((n + 255) / 256, 152u * 16u);
+    if (blocks) k_inverse<<<blocks, 256, 0, s>>>(sorted, inv, n, check);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_occupancy(const uint32_t* delims, uint64_t nbins, uint32_t crowd, unsigned long long* out,
                              int blocks, cudaStream_t s) {

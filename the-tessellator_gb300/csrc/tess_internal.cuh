@@ -172,7 +172,7 @@ struct GridBuffers {
     uint32_t* delims;           // total_bins + 1
     uint32_t* scan_tmp;         // block sums
     uint32_t* sorted;
-    uint32_t* inv;              // point -> sorted position
+    uint32_t* inv;              // point -> sorted position, or null (built on demand)
     double* spx;
     double* spy;
     double* spz;
@@ -193,6 +193,8 @@ constexpr int kScanThreads = 1024;
 // scatter run (fork after the grid parameters, join before returning).
 cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s, cudaStream_t side = nullptr,
                               cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
+// inv[sorted[s]] = s for s < n (the point -> sorted position map, on demand).
+cudaError_t launch_inverse(const uint32_t* sorted, uint32_t* inv, uint32_t n, int* check, cudaStream_t s);
 // out[0] = most points in one bin, out[1] = points in bins of >= crowd points
 // (every bin of every diagram of the set)
 cudaError_t launch_occupancy(const uint32_t* delims, uint64_t nbins, uint32_t crowd, unsigned long long* out,
