@@ -48,14 +48,14 @@ WORKLOADS = {
 RADIUS_METRIC = "radius queries/sec on 1 GB300 (find_neighbors_in_real_radius, FP64, exact)"
 
 # DRAM traffic per launch from ncu captures of the same kernels on GB300.  The
-# clipping pass was captured at 1,000,000 cells (dram__bytes.sum.per_second
-# 14.72 GB/s over 16.96 ms: 249.8 MB) and is scaled by cells: its traffic is
-# its output plus L2 misses, both per cell.  The radius passes were captured at
-# full size (16,777,216 queries, radius 0.006).
-NCU_CLIP_BYTES_PER_CELL = 14.724912e9 * 16.963904e-3 / 1_000_000
+# clipping pass was captured at 1,000,000 cells (dram__bytes_read.sum 79.7 MB +
+# dram__bytes_write.sum 171.0 MB in 16.44 ms) and is scaled by cells: its
+# traffic is its output plus L2 misses, both per cell.  The radius passes were
+# captured at full size (16,777,216 queries, radius 0.006).
+NCU_CLIP_BYTES_PER_CELL = (79.678720e6 + 171.049728e6) / 1_000_000
 # Warp instructions of the same capture (smsp__inst_executed.sum), per cell: the
 # kernel is bound by instruction issue, so this gives its issue roofline.
-NCU_CLIP_INST_PER_CELL = 13_255_807_231 / 1_000_000
+NCU_CLIP_INST_PER_CELL = 12_904_248_352 / 1_000_000
 NCU_RADIUS_BYTES = {"count": 3.846207488e9 + 0.50285184e9, "fill": 6.337812736e9 + 1.53743616e9}
 # DRAM traffic of the 11 binning launches (read 651.8 MB + write 183.7 MB) at
 # 4,194,304 uniform points, scaled by points: every term is per point or per bin.
