@@ -1183,8 +1183,6 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         return ST_OK;
     };
 
-    // Cut by every point of the lane's two bins, given as sorted ranges
-    // [begA, begA + cntA) and [begB, begB + cntB).
     // Cut by every point of the lanes' bins, given as sorted ranges
     // [beg, beg + cnt), in lane order; or (direct) by one window of the
     // lanes' seeds of a crowded bin (S.sd*).
