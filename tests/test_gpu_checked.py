@@ -57,12 +57,11 @@ def _child():
     """Runs in the child process: every case through the checked library."""
     sys.path.insert(0, os.path.join(ROOT, "the-tessellator_gb300"))
     sys.path.insert(0, ROOT)
-    import tessellator._capi as capi
-
-    capi.LIB_PATH = os.environ["TESS_CHECKED_LIB"]
     import oracle
     import tessellator as T
     from oracle import report
+
+    assert T._capi.LIB_PATH == os.environ["TESS_LIB"]
 
     box = T.Polyhedron(0, 0, 0, 1, 1, 1)
     for name, pts, precs, flags in _cases():
@@ -114,7 +113,7 @@ def test_checked_build_stays_in_bounds():
     import build_lib
 
     lib = build_lib.build(checked=True)
-    env = dict(os.environ, TESS_CHECKED_LIB=lib, TESS_CHECKED_CHILD="1")
+    env = dict(os.environ, TESS_LIB=lib, TESS_CHECKED_CHILD="1")
     r = subprocess.run([sys.executable, os.path.abspath(__file__)], env=env, capture_output=True, text=True,
                        timeout=900)
     print(r.stdout)

@@ -9,7 +9,10 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libtessgpu.so")
+# $TESS_LIB selects another build of the library, e.g. libtessgpu_checked.so
+# (every device index bounds-checked; calls that met a bad one fail with
+# TESS_E_CHECK).
+LIB_PATH = os.environ.get("TESS_LIB") or os.path.join(HERE, "libtessgpu.so")
 
 TESS_OK, TESS_E_INVALID, TESS_E_CUDA, TESS_E_CAPACITY = 0, 1, 2, 3
 TESS_E_OVERFLOW, TESS_E_STATE, TESS_E_NOMEM, TESS_E_LIMIT, TESS_E_CHECK = 4, 5, 6, 7, 8
