@@ -268,6 +268,31 @@ tess_status tess_neighbors_csr(tess_diagram* d, uint64_t* offs, int32_t* nbr, do
  * destroy): volumes[n], offs[n+1], nbr[total], area[total]. */
 tess_status tess_results_device(tess_diagram* d, const double** volumes, const uint64_t** offs,
                                 const int32_t** nbr, const double** area, size_t* total);
+/* tess_diagram_compute_all with every cell's results delivered to the
+ * caller's buffers: the Cell outputs of interface.rs:337-416 (volume,
+ * neighbours, face areas) for all cells, as Diagram::compute_voronoi_cell
+ * (interface.rs:257-334) gives them one at a time.  The kernels write each
+ * cell's faces (neighbour id, area; sorted by id, as in the CSR) into the face
+ * pool face_nbr/face_area[face_cap] as the cell finishes, so on a host buffer
+ * the faces cross the host link during the compute instead of after it.  Cell
+ * i's faces are face_nbr/face_area[face_start[i] .. face_start[i] +
+ * face_count[i]); volumes[n], face_start[n], face_count[n] are written at the
+ * end.  The two pool buffers must have a device address: pinned host memory
+ * (tess_host_alloc, cudaHostAlloc, cudaHostRegister), device or managed
+ * memory; pageable memory is TESS_E_INVALID.  The other three may be any
+ * memory.  *faces_used (may be NULL) receives the pool positions used.  A pool
+ * too small is TESS_E_CAPACITY with *faces_used = the size needed (the diagram
+ * is then not computed).  Afterwards the faces exist only in the caller's
+ * buffers: tess_neighbors_csr, tess_results_device and the per-cell face
+ * queries return TESS_E_STATE until the next tess_diagram_compute_all. */
+tess_status tess_diagram_compute_all_to_host(tess_diagram* d, tess_precision precision, double search_radius,
+                                             int64_t target_group, double* volumes, uint64_t* face_start,
+                                             uint32_t* face_count, int32_t* face_nbr, double* face_area,
+                                             size_t face_cap, size_t* faces_used);
+/* Pinned, device-mapped host memory for the buffers above (cudaHostAlloc);
+ * bytes = 0 gives NULL.  Free with tess_host_free (NULL is a no-op). */
+tess_status tess_host_alloc(size_t bytes, void** ptr);
+tess_status tess_host_free(void* ptr);
 
 /* ---- fixed-radius queries on the bin grid ---- */
 /* Batched over nq queries.  Results come back as CSR: offs[nq+1] and out[total]

@@ -99,6 +99,12 @@ extern "C" {
                               cap: usize, total: *mut usize) -> tess_status;
     pub fn tess_results_device(d: *mut tess_diagram, volumes: *mut *const f64, offs: *mut *const u64,
                                nbr: *mut *const i32, area: *mut *const f64, total: *mut usize) -> tess_status;
+    pub fn tess_diagram_compute_all_to_host(d: *mut tess_diagram, precision: c_int, search_radius: f64,
+                                            target_group: i64, volumes: *mut f64, face_start: *mut u64,
+                                            face_count: *mut u32, face_nbr: *mut i32, face_area: *mut f64,
+                                            face_cap: usize, faces_used: *mut usize) -> tess_status;
+    pub fn tess_host_alloc(bytes: usize, ptr: *mut *mut c_void) -> tess_status;
+    pub fn tess_host_free(ptr: *mut c_void) -> tess_status;
     // fixed-radius queries (celery.rs:753-855, interface.rs:348-365)
     pub fn tess_find_cells_in_radius(d: *mut tess_diagram, xyz: *const f64, nq: usize, radius: f64,
                                      on_device: c_int, offs: *mut u64, cells: *mut u32, cap: usize,

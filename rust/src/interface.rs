@@ -19,7 +19,7 @@
 //! the cell's site, as the reference leaves its polyhedron translated.
 use crate::gpu_ffi::*;
 use std::ffi::CStr;
-use std::os::raw::c_char;
+use std::os::raw::{c_char, c_void};
 use std::ptr;
 
 /// A failed call: its status code and the library's message.
@@ -162,6 +162,37 @@ impl Diagram {
         Ok(t)
     }
 
+    /// `compute_all` with every cell's faces written into a pinned host pool
+    /// while the cells finish (tess_diagram_compute_all_to_host).  `face_cap`
+    /// sizes the pool; a pool too small is grown once to the size the call
+    /// reports.
+    pub fn compute_all_to_host(&mut self, precision: Precision, search_radius: Option<f64>,
+                               target_group: Option<usize>, face_cap: usize) -> Result<HostResults, Error> {
+        let mut cap = face_cap.max(1);
+        for _ in 0..2 {
+            let nbr = PinnedBuf::<i32>::new(cap)?;
+            let area = PinnedBuf::<f64>::new(cap)?;
+            let mut volumes = vec![0.0f64; self.n];
+            let mut face_start = vec![0u64; self.n];
+            let mut face_count = vec![0u32; self.n];
+            let mut used = 0usize;
+            let st = unsafe {
+                tess_diagram_compute_all_to_host(self.h, precision.code(), radius_arg(search_radius),
+                                                 group_arg(target_group), volumes.as_mut_ptr(),
+                                                 face_start.as_mut_ptr(), face_count.as_mut_ptr(), nbr.ptr,
+                                                 area.ptr, cap, &mut used)
+            };
+            if st == TESS_E_CAPACITY {
+                cap = used;
+                continue;
+            }
+            check(st)?;
+            return Ok(HostResults { volumes, face_start, face_count, face_nbr: nbr, face_area: area,
+                                    faces_used: used });
+        }
+        Err(Error { status: TESS_E_CAPACITY, message: last_error() })
+    }
+
     /// get_cell_at_index (interface.rs:186-208).
     pub fn get_cell_at_index(&self, index: usize, polyhedron: Polyhedron, search_radius: Option<f64>,
                              target_group: Option<usize>) -> Cell {
@@ -210,6 +241,55 @@ impl Diagram {
 impl Drop for Diagram {
     fn drop(&mut self) {
         unsafe { tess_diagram_destroy(self.h) };
+    }
+}
+
+/// Pinned, device-mapped host memory (tess_host_alloc).
+pub struct PinnedBuf<T: Copy> {
+    ptr: *mut T,
+    len: usize,
+}
+
+impl<T: Copy> PinnedBuf<T> {
+    pub fn new(len: usize) -> Result<Self, Error> {
+        let mut p: *mut c_void = ptr::null_mut();
+        check(unsafe { tess_host_alloc(len * std::mem::size_of::<T>(), &mut p) })?;
+        Ok(PinnedBuf { ptr: p as *mut T, len })
+    }
+
+    pub fn as_slice(&self) -> &[T] {
+        if self.len == 0 {
+            &[]
+        } else {
+            unsafe { std::slice::from_raw_parts(self.ptr, self.len) }
+        }
+    }
+}
+
+impl<T: Copy> Drop for PinnedBuf<T> {
+    fn drop(&mut self) {
+        unsafe { tess_host_free(self.ptr as *mut c_void) };
+    }
+}
+
+/// Every cell's results from `compute_all_to_host`: cell i's faces are
+/// `face_nbr` / `face_area` at `face_start[i] .. face_start[i] + face_count[i]`
+/// (sorted by neighbour id, walls -1..-6).
+pub struct HostResults {
+    pub volumes: Vec<f64>,
+    pub face_start: Vec<u64>,
+    pub face_count: Vec<u32>,
+    pub face_nbr: PinnedBuf<i32>,
+    pub face_area: PinnedBuf<f64>,
+    pub faces_used: usize,
+}
+
+impl HostResults {
+    /// Neighbour ids and areas of cell i.
+    pub fn faces(&self, i: usize) -> (&[i32], &[f64]) {
+        let a = self.face_start[i] as usize;
+        let b = a + self.face_count[i] as usize;
+        (&self.face_nbr.as_slice()[a..b], &self.face_area.as_slice()[a..b])
     }
 }
 

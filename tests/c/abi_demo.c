@@ -75,6 +75,33 @@ int main(void) {
         for (size_t f = 0; f < nn; ++f)
             if (cn[f] != nbr[offs[c] + f]) return fail("cell neighbour ids");
         printf("precision %d: %d cells, %zu faces, volume sum %.15f\n", (int)precs[q], N, total, sum);
+        /* the same cells with the faces written into a pinned host pool */
+        {
+            const size_t cap = total + 64;
+            void *pn = NULL, *pa = NULL;
+            double* hv = (double*)malloc(sizeof(double) * N);
+            uint64_t* hs = (uint64_t*)malloc(sizeof(uint64_t) * N);
+            uint32_t* hc = (uint32_t*)malloc(sizeof(uint32_t) * N);
+            size_t used = 0;
+            if (tess_host_alloc(sizeof(int32_t) * cap, &pn) != TESS_OK ||
+                tess_host_alloc(sizeof(double) * cap, &pa) != TESS_OK)
+                return fail("host alloc");
+            if (tess_diagram_compute_all_to_host(d, precs[q], -1.0, -1, hv, hs, hc, (int32_t*)pn, (double*)pa, cap,
+                                                 &used) != TESS_OK)
+                return fail("compute_all_to_host");
+            for (int i = 0; i < N; ++i) {
+                if (hv[i] != vol[i] || hc[i] != offs[i + 1] - offs[i]) return fail("to_host volume or count");
+                for (uint32_t f = 0; f < hc[i]; ++f)
+                    if (((int32_t*)pn)[hs[i] + f] != nbr[offs[i] + f] || ((double*)pa)[hs[i] + f] != area[offs[i] + f])
+                        return fail("to_host faces");
+            }
+            if (tess_neighbors_csr(d, offs, NULL, NULL, 0, &total) != TESS_E_STATE) return fail("csr after to_host");
+            tess_host_free(pn);
+            tess_host_free(pa);
+            free(hv);
+            free(hs);
+            free(hc);
+        }
         free(nbr);
         free(area);
     }

@@ -162,6 +162,11 @@ struct Engine {
     int32_t* d_fnbr = nullptr;
     double* d_farea = nullptr;
     uint64_t face_cap = 0;
+    // tess_diagram_compute_all_to_host: the pool is the caller's buffer for one
+    // compute (never regrown), and the faces of that compute are on the host
+    bool pool_fixed = false;
+    bool faces_on_host = false;
+    uint64_t pool_need = 0;
     unsigned long long* d_fcursor = nullptr;
     uint32_t* d_list[L_COUNT] = {};
     unsigned* d_counters = nullptr;   // [0..15] cursors, [16..31] list counts
@@ -685,6 +690,12 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
             E.computed = false;
             return fail(TESS_E_INVALID, "input coordinates must be finite");
         }
+        if (used > E.face_cap && E.pool_fixed) {
+            // the caller's pool: report the size needed
+            E.pool_need = used;
+            E.computed = false;
+            return fail(TESS_E_CAPACITY, "%llu faces, face_cap %llu", used, (unsigned long long)E.face_cap);
+        }
         if (used > E.face_cap) {
             // face pool too small: grow and recompute
             dfree(E.d_fnbr);
@@ -719,6 +730,7 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
         }
         E.computed = true;
         E.csr_valid = false;
+        E.faces_on_host = E.pool_fixed;
         E.last_precision = precision;
         E.last_radius = radius;
         E.last_group = group;
@@ -745,6 +757,8 @@ tess_status engine_compute(Engine& E, int precision, double radius, int64_t grou
 
 tess_status engine_csr(Engine& E) {
     if (!E.computed) return fail(TESS_E_STATE, "compute_all has not run");
+    if (E.faces_on_host)
+        return fail(TESS_E_STATE, "the last compute wrote its faces to the caller's buffers (compute_all_to_host)");
     if (E.csr_valid) return TESS_OK;
     CU(cudaSetDevice(E.device));
     TimingEvents ev;
@@ -899,6 +913,7 @@ tess_status time_sample(Engine& E, int precision, uint32_t m, float* ms) {
             *ms = ev.ms(0, 1);
             return TESS_OK;
         }
+        if (E.pool_fixed) return fail(TESS_E_CAPACITY, "face pool too small for the tuning sample");
         dfree(E.d_fnbr);
         dfree(E.d_farea);
         E.face_cap = std::max<uint64_t>(2 * E.face_cap, used + used / 4 + 4096);
@@ -1385,6 +1400,90 @@ tess_status tess_diagram_compute_all(tess_diagram* d, tess_precision precision, 
     return engine_compute(d->E, (int)precision, search_radius, target_group);
 }
 
+// The device address of a buffer the kernels may write: pinned host memory
+// (cudaHostAlloc, cudaHostRegister, tess_host_alloc), device or managed
+// memory.  Pageable host memory has none.
+static tess_status device_address(void* p, void** out, const char* what) {
+    cudaPointerAttributes a{};
+    const cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess || a.type == cudaMemoryTypeUnregistered || !a.devicePointer) {
+        cudaGetLastError();
+        return fail(TESS_E_INVALID, "%s is not pinned host, device or managed memory", what);
+    }
+    *out = a.devicePointer;
+    return TESS_OK;
+}
+
+tess_status tess_diagram_compute_all_to_host(tess_diagram* d, tess_precision precision, double search_radius,
+                                             int64_t target_group, double* volumes, uint64_t* face_start,
+                                             uint32_t* face_count, int32_t* face_nbr, double* face_area,
+                                             size_t face_cap, size_t* faces_used) {
+    if (!d) return fail(TESS_E_INVALID, "diagram is NULL");
+    if (!volumes || !face_start || !face_count || !face_nbr || !face_area)
+        return fail(TESS_E_INVALID, "NULL output buffer");
+    Engine& E = d->E;
+    CU(cudaSetDevice(E.device));
+    void *dn = nullptr, *da = nullptr;
+    TRY(device_address(face_nbr, &dn, "face_nbr"));
+    TRY(device_address(face_area, &da, "face_area"));
+    // a pending autotune times its samples in the library's own pool
+    if (E.built && (E.cfg.flags & TESS_FLAG_AUTOTUNE) && !E.tuned &&
+        (precision == TESS_PRECISION_FP64 || precision == TESS_PRECISION_FP32_GUARD ||
+         precision == TESS_PRECISION_MIXED))
+        TRY(engine_autotune(E, (int)precision, false, nullptr, nullptr));
+    // the kernels write each cell's faces straight into the caller's pool as
+    // the cell finishes, so the faces cross the host link during the compute
+    int32_t* const own_nbr = E.d_fnbr;
+    double* const own_area = E.d_farea;
+    const uint64_t own_cap = E.face_cap;
+    E.d_fnbr = static_cast<int32_t*>(dn);
+    E.d_farea = static_cast<double*>(da);
+    E.face_cap = face_cap;
+    E.pool_fixed = true;
+    E.pool_need = 0;
+    const tess_status st = engine_compute(E, (int)precision, search_radius, target_group);
+    E.d_fnbr = own_nbr;
+    E.d_farea = own_area;
+    E.face_cap = own_cap;
+    E.pool_fixed = false;
+    if (faces_used) *faces_used = st == TESS_E_CAPACITY ? E.pool_need : E.stats.faces;
+    if (st != TESS_OK && st != TESS_E_OVERFLOW) {
+        if (st == TESS_E_CAPACITY) E.faces_on_host = false;
+        return st;
+    }
+    // the per-cell results (failed cells: volume 0, no faces)
+    const size_t n = d->n;
+    CU(cudaMemcpyAsync(volumes, E.d_vol, sizeof(double) * n, cudaMemcpyDefault, E.stream));
+    CU(cudaMemcpyAsync(face_start, E.d_fstart, sizeof(uint64_t) * n, cudaMemcpyDefault, E.stream));
+    CU(cudaMemcpyAsync(face_count, E.d_nface, sizeof(uint32_t) * n, cudaMemcpyDefault, E.stream));
+    CU(cudaStreamSynchronize(E.stream));
+    return st;
+}
+
+tess_status tess_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr) return fail(TESS_E_INVALID, "ptr is NULL");
+    *ptr = nullptr;
+    if (bytes == 0) return TESS_OK;
+    const cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocMapped | cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return fail(e == cudaErrorMemoryAllocation ? TESS_E_NOMEM : TESS_E_CUDA, "cudaHostAlloc(%zu): %s", bytes,
+                    cudaGetErrorString(e));
+    }
+    return TESS_OK;
+}
+
+tess_status tess_host_free(void* ptr) {
+    if (!ptr) return TESS_OK;
+    const cudaError_t e = cudaFreeHost(ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(TESS_E_CUDA, "cudaFreeHost: %s", cudaGetErrorString(e));
+    }
+    return TESS_OK;
+}
+
 tess_status tess_diagram_stats(const tess_diagram* d, tess_stats* out) {
     if (!d || !out) return fail(TESS_E_INVALID, "NULL argument");
     *out = d->E.stats;
@@ -1445,6 +1544,8 @@ tess_status tess_cell_volume(const tess_diagram* d, size_t i, double* volume) {
 tess_status tess_cell_faces(const tess_diagram* d, size_t i, int32_t* nbr, double* area, size_t cap,
                             size_t* count) {
     TRY(cell_check(d, i));
+    if (d->E.faces_on_host)
+        return fail(TESS_E_STATE, "the last compute wrote its faces to the caller's buffers (compute_all_to_host)");
     CU(cudaSetDevice(d->E.device));
     uint32_t nf = 0;
     uint64_t fs = 0;

@@ -13,8 +13,9 @@ The classes mirror the reference's public types:
                  (interface.rs:393-416)
 
 plus the bulk path the GPU is built for: ``Diagram.compute_all`` with
-``volumes()`` and ``neighbors_csr()``, and ``Batch`` for many diagrams in one
-CUDA-graph launch.  Every computation runs in libtessgpu.so on the GPU; there
+``volumes()`` and ``neighbors_csr()`` (or ``compute_all_to_host``, which
+streams every cell's faces into pinned host memory during the compute), and
+``Batch`` for many diagrams in one CUDA-graph launch.  Every computation runs in libtessgpu.so on the GPU; there
 is no CPU fallback.
 
 Conventions: indices are the caller's original indices; box faces report
@@ -31,10 +32,11 @@ from typing import List, Optional
 import numpy as np
 
 from ._capi import (FLAG_AUTOTUNE, FLAG_COUNTERS, FLAG_NO_CAPACITY_RERUN, FLAG_SMALL_FACE_POOL, FLAG_TIMING,
-                    PRECISION_FP32_GUARD, PRECISION_FP64, PRECISION_MIXED,
+                    PRECISION_FP32_GUARD, PRECISION_FP64, PRECISION_MIXED, TESS_E_CAPACITY,
                     CellGeometry, Config, Stats, TessError, Tuning, check, default_config, last_error, lib)
 
 __all__ = ["Polyhedron", "Diagram", "Cell", "VoronoiFace", "Batch", "DeviceArray", "TessError", "Config",
+           "pinned_empty", "HostResults",
            "default_config", "PRECISION_FP64", "PRECISION_FP32_GUARD", "PRECISION_MIXED", "FLAG_TIMING",
            "FLAG_COUNTERS", "FLAG_SMALL_FACE_POOL", "FLAG_NO_CAPACITY_RERUN", "FLAG_AUTOTUNE", "lib",
            "last_error"]
@@ -63,6 +65,54 @@ def _radius(r: Optional[float]) -> float:
 
 def _group(g: Optional[int]) -> int:
     return -1 if g is None else int(g)
+
+
+class _PinnedBlock:
+    """Pinned, device-mapped host memory from tess_host_alloc; freed when the
+    last array over it is gone."""
+
+    def __init__(self, nbytes: int):
+        self.ptr = C.c_void_p()
+        check(lib().tess_host_alloc(max(int(nbytes), 1), C.byref(self.ptr)))
+        self.nbytes = max(int(nbytes), 1)
+
+    def __del__(self):
+        if getattr(self, "ptr", None) is not None and self.ptr.value:
+            lib().tess_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+
+def pinned_empty(n: int, dtype) -> np.ndarray:
+    """An uninitialised numpy array of n elements in pinned, device-mapped host
+    memory (tess_host_alloc): the face pool of compute_all_to_host."""
+    dt = np.dtype(dtype)
+    blk = _PinnedBlock(int(n) * dt.itemsize)
+    buf = (C.c_char * blk.nbytes).from_address(blk.ptr.value)
+    buf._owner = blk   # the array keeps the buffer, the buffer the block
+    return np.frombuffer(buf, dtype=dt, count=int(n))
+
+
+class HostResults:
+    """Every cell's results from Diagram.compute_all_to_host: cell i's faces
+    are face_nbr / face_area[face_start[i] : face_start[i] + face_count[i]]
+    (sorted by neighbour id, walls -1..-6)."""
+
+    def __init__(self, volumes, face_start, face_count, face_nbr, face_area, faces_used):
+        self.volumes, self.face_start, self.face_count = volumes, face_start, face_count
+        self.face_nbr, self.face_area, self.faces_used = face_nbr, face_area, faces_used
+
+    def faces(self, i: int):
+        a = int(self.face_start[i])
+        b = a + int(self.face_count[i])
+        return self.face_nbr[a:b], self.face_area[a:b]
+
+    def csr(self):
+        """The same results as Diagram.neighbors_csr: (offsets[n+1], ids, areas)."""
+        offs = np.zeros(len(self.volumes) + 1, dtype=np.uint64)
+        np.cumsum(self.face_count, out=offs[1:])
+        idx = (np.repeat(self.face_start.astype(np.int64) - offs[:-1].astype(np.int64), self.face_count.astype(np.int64))
+               + np.arange(int(offs[-1]), dtype=np.int64))
+        return offs, self.face_nbr[idx], self.face_area[idx]
 
 
 class DeviceArray:
@@ -193,6 +243,43 @@ class Diagram:
         cp = None if cache_path is None else cache_path.encode()
         check(lib().tess_diagram_autotune(self._h, _prec(precision), cp, C.byref(t)))
         return t.as_dict()
+
+    def compute_all_to_host(self, precision="fp32", search_radius: Optional[float] = None,
+                            target_group: Optional[int] = None, face_pool=None) -> "HostResults":
+        """compute_all with every cell's faces written by the GPU into a pinned
+        host pool as the cells finish (tess_diagram_compute_all_to_host).
+
+        ``face_pool``: (ids int32, areas float64) arrays from ``pinned_empty``
+        of equal length to reuse; None allocates one (grown and retried once
+        when the call reports a larger size).  The faces then exist only in
+        that pool: neighbors_csr and the per-cell face queries need another
+        compute_all."""
+        L = lib()
+        vol = np.empty(self.n, dtype=np.float64)
+        fstart = np.empty(self.n, dtype=np.uint64)
+        fcount = np.empty(self.n, dtype=np.uint32)
+        used = C.c_size_t(0)
+        if face_pool is None:
+            cap = 20 * self.n + 1024
+            face_pool = (pinned_empty(cap, np.int32), pinned_empty(cap, np.float64))
+            retry = True
+        else:
+            retry = False
+        for _ in range(2):
+            nbr, area = face_pool
+            if len(nbr) != len(area) or nbr.dtype != np.int32 or area.dtype != np.float64:
+                raise ValueError("face_pool: two arrays of equal length, int32 and float64")
+            st = L.tess_diagram_compute_all_to_host(
+                self._h, _prec(precision), _radius(search_radius), _group(target_group), vol.ctypes.data,
+                fstart.ctypes.data, fcount.ctypes.data, nbr.ctypes.data, area.ctypes.data, len(nbr),
+                C.byref(used))
+            if st == TESS_E_CAPACITY and retry:   # the size needed is in used
+                face_pool = (pinned_empty(used.value, np.int32), pinned_empty(used.value, np.float64))
+                retry = False
+                continue
+            check(st)
+            break
+        return HostResults(vol, fstart, fcount, face_pool[0], face_pool[1], used.value)
 
     def volumes(self) -> np.ndarray:
         out = np.empty(self.n, dtype=np.float64)

@@ -36,6 +36,7 @@ EXPORTS = (
     "tess_cell_volume", "tess_cell_neighbors", "tess_cell_faces", "tess_cell_vertices",
     "tess_cell_face_vertices", "tess_cell_original_index", "tess_cell_compute",
     "tess_cell_compute_at", "tess_volumes", "tess_neighbors_csr", "tess_results_device",
+    "tess_diagram_compute_all_to_host", "tess_host_alloc", "tess_host_free",
     "tess_find_cells_in_radius", "tess_find_neighbors_in_radius", "tess_neighbor_cloud",
     "tess_neighbor_cloud_at",
     "tess_batch_create", "tess_batch_compute", "tess_batch_update_points", "tess_batch_stats", "tess_batch_volumes",
@@ -130,6 +131,10 @@ def lib():
         "tess_volumes": (st, [vp, dp]),
         "tess_neighbors_csr": (st, [vp, u64p, i32p, dp, C.c_size_t, szp]),
         "tess_results_device": (st, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), szp]),
+        "tess_diagram_compute_all_to_host": (st, [vp, C.c_int, C.c_double, C.c_int64, vp, vp, vp, vp, vp,
+                                                  C.c_size_t, szp]),
+        "tess_host_alloc": (st, [C.c_size_t, C.POINTER(vp)]),
+        "tess_host_free": (st, [vp]),
         "tess_find_cells_in_radius": (st, [vp, vp, C.c_size_t, C.c_double, C.c_int, vp, vp, C.c_size_t, szp]),
         "tess_find_neighbors_in_radius": (st, [vp, vp, C.c_size_t, C.c_double, C.c_int, C.c_int, vp, vp,
                                                C.c_size_t, szp]),
