@@ -718,8 +718,9 @@ def clustered_leg(args, T, cfg, stream, local, rank):
 
 def batched_leg(args, T, cfg, stream, local, rank):
     """C4: 4,096 diagrams (n log-uniform in [64, 65536], own boxes), FP32 +
-    guard, one CUDA graph per compute; e2e through the C ABI (points in,
-    volumes and CSR out); parity on evenly spaced whole diagrams."""
+    guard, one CUDA graph per compute; e2e through the C ABI (points in, every
+    cell's results out: tess_batch_compute_to_host, with the read-back path
+    timed beside it); parity on evenly spaced whole diagrams."""
     import torch
 
     pts, (offs, boxes) = make_points("batched")
@@ -749,12 +750,42 @@ def batched_leg(args, T, cfg, stream, local, rank):
                                                      dp(area_h, C.c_double), cap, C.byref(tot)))
             return tot.value
 
+        # the read-back path (its results feed the parity report), then the
+        # headline: the faces written into a pinned host pool during the
+        # compute (tess_batch_compute_to_host)
         step_e2e()
+        csr_steps = max(1, min(2, steps))
+        t0 = time.perf_counter()
+        for _ in range(csr_steps):
+            tot = step_e2e()
+        csr_s = (time.perf_counter() - t0) / csr_steps
+        res = (vol_h.numpy(), offs_h.numpy(), nbr_h.numpy()[:tot], area_h.numpy()[:tot])
+        hvol = torch.empty(n, dtype=torch.float64).pin_memory()
+        hfs = torch.empty(n, dtype=torch.int64).pin_memory()
+        hfc = torch.empty(n, dtype=torch.int32).pin_memory()
+        hnbr = torch.empty(cap, dtype=torch.int32).pin_memory()
+        harea = torch.empty(cap, dtype=torch.float64).pin_memory()
+
+        def step_host():
+            T._capi.check(L.tess_batch_update_points(b._h, C.c_void_p(host.data_ptr()), 0))
+            used = C.c_size_t(0)
+            T._capi.check(L.tess_batch_compute_to_host(b._h, T._PREC["fp32"], hvol.data_ptr(), hfs.data_ptr(),
+                                                       hfc.data_ptr(), hnbr.data_ptr(), harea.data_ptr(), cap,
+                                                       C.byref(used)))
+            return used.value
+
+        step_host()
         t0 = time.perf_counter()
         for _ in range(steps):
-            tot = step_e2e()
+            used = step_host()
         e2e_s = (time.perf_counter() - t0) / steps
-        res = (vol_h.numpy(), offs_h.numpy(), nbr_h.numpy()[:tot], area_h.numpy()[:tot])
+        pick = np.unique(np.linspace(0, n - 1, min(n, 20000)).astype(np.int64))
+        fsn, fcn, hn, ha = hfs.numpy(), hfc.numpy(), hnbr.numpy(), harea.numpy()
+        same = bool(np.array_equal(hvol.numpy()[pick], res[0][pick]))
+        for i in pick:
+            a, e = int(fsn[i]), int(fsn[i]) + int(fcn[i])
+            o0, o1 = int(res[1][i]), int(res[1][i + 1])
+            same &= bool(np.array_equal(hn[a:e], res[2][o0:o1]) and np.array_equal(ha[a:e], res[3][o0:o1]))
         sizes = np.diff(offs.astype(np.int64))
         leg = {"workload": WORKLOADS["batched"]["desc"], "diagrams": nd, "cells": n,
                "value": n / (mms / 1e3), "unit": "cells/s", "ms_per_step": mms, "steps": steps,
@@ -763,8 +794,14 @@ def batched_leg(args, T, cfg, stream, local, rank):
                "reruns": {"fp32_hybrid": int(st["rerun_fp64"]), "fp64_full": int(st["rerun_fp64_full"]),
                           "capacity": int(st["rerun_capacity"]), "failed": int(st["failed"])},
                "e2e": {"value": n / e2e_s, "unit": "cells/s", "ms_per_step": e2e_s * 1e3,
-                       "h2d_bytes_per_step": int(pts.nbytes),
-                       "d2h_bytes_per_step": int(8 * n + 8 * (n + 1) + 12 * len(res[2]))}}
+                       "h2d_bytes_per_step": int(pts.nbytes), "d2h_bytes_per_step": int(12 * used + 20 * n),
+                       "calls": "tess_batch_update_points, tess_batch_compute_to_host",
+                       "same_as_csr_path": {"cells_checked": int(len(pick)), "identical": same},
+                       "csr_path": {"value": n / csr_s, "unit": "cells/s", "ms_per_step": csr_s * 1e3,
+                                    "steps": csr_steps,
+                                    "d2h_bytes_per_step": int(8 * n + 8 * (n + 1) + 12 * len(res[2])),
+                                    "calls": "tess_batch_update_points, tess_batch_compute, tess_batch_volumes, "
+                                             "tess_batch_neighbors_csr"}}}
     finally:
         b.close()
     vol, go, gn, ga = res

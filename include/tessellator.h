@@ -351,6 +351,14 @@ tess_status tess_batch_create(size_t ndiag, const uint64_t* pt_offsets, const do
 /* Bin and clip every diagram.  The sequence of launches is captured in a CUDA
  * graph on first use and replayed afterwards. */
 tess_status tess_batch_compute(tess_batch* b, tess_precision precision);
+/* tess_batch_compute with the faces written into the caller's pool as the
+ * cells finish, as tess_diagram_compute_all_to_host: volumes, face_start and
+ * face_count over all points (total), neighbour ids local to each diagram.
+ * The graph captured for a pool is kept while the pool, its capacity and the
+ * precision stay the same. */
+tess_status tess_batch_compute_to_host(tess_batch* b, tess_precision precision, double* volumes,
+                                       uint64_t* face_start, uint32_t* face_count, int32_t* face_nbr,
+                                       double* face_area, size_t face_cap, size_t* faces_used);
 /* Replace every diagram's points (same offsets and boxes), from host memory or
  * (on_device != 0) device memory; the next tess_batch_compute bins them
  * again.  The batch form of Celery::reset (celery.rs:253-266) over

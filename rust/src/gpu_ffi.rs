@@ -122,6 +122,9 @@ extern "C" {
     pub fn tess_batch_create(ndiag: usize, pt_offsets: *const u64, xyz: *const f64, boxes: *const f64,
                              cfg: *const tess_config, out: *mut *mut tess_batch) -> tess_status;
     pub fn tess_batch_compute(b: *mut tess_batch, precision: c_int) -> tess_status;
+    pub fn tess_batch_compute_to_host(b: *mut tess_batch, precision: c_int, volumes: *mut f64, face_start: *mut u64,
+                                      face_count: *mut u32, face_nbr: *mut i32, face_area: *mut f64,
+                                      face_cap: usize, faces_used: *mut usize) -> tess_status;
     pub fn tess_batch_update_points(b: *mut tess_batch, xyz: *const f64, on_device: c_int) -> tess_status;
     pub fn tess_batch_stats(b: *const tess_batch, out: *mut tess_stats) -> tess_status;
     pub fn tess_batch_volumes(b: *mut tess_batch, volumes: *mut f64) -> tess_status;

@@ -168,29 +168,10 @@ impl Diagram {
     /// reports.
     pub fn compute_all_to_host(&mut self, precision: Precision, search_radius: Option<f64>,
                                target_group: Option<usize>, face_cap: usize) -> Result<HostResults, Error> {
-        let mut cap = face_cap.max(1);
-        for _ in 0..2 {
-            let nbr = PinnedBuf::<i32>::new(cap)?;
-            let area = PinnedBuf::<f64>::new(cap)?;
-            let mut volumes = vec![0.0f64; self.n];
-            let mut face_start = vec![0u64; self.n];
-            let mut face_count = vec![0u32; self.n];
-            let mut used = 0usize;
-            let st = unsafe {
-                tess_diagram_compute_all_to_host(self.h, precision.code(), radius_arg(search_radius),
-                                                 group_arg(target_group), volumes.as_mut_ptr(),
-                                                 face_start.as_mut_ptr(), face_count.as_mut_ptr(), nbr.ptr,
-                                                 area.ptr, cap, &mut used)
-            };
-            if st == TESS_E_CAPACITY {
-                cap = used;
-                continue;
-            }
-            check(st)?;
-            return Ok(HostResults { volumes, face_start, face_count, face_nbr: nbr, face_area: area,
-                                    faces_used: used });
-        }
-        Err(Error { status: TESS_E_CAPACITY, message: last_error() })
+        let (h, p, r, g) = (self.h, precision.code(), radius_arg(search_radius), group_arg(target_group));
+        to_host(self.n, face_cap, |v, fs, fc, nb, ar, cap, used| unsafe {
+            tess_diagram_compute_all_to_host(h, p, r, g, v, fs, fc, nb, ar, cap, used)
+        })
     }
 
     /// get_cell_at_index (interface.rs:186-208).
@@ -242,6 +223,32 @@ impl Drop for Diagram {
     fn drop(&mut self) {
         unsafe { tess_diagram_destroy(self.h) };
     }
+}
+
+/// Runs a to-host compute into fresh per-cell arrays and a pinned face pool
+/// of `face_cap`, grown once to the size a TESS_E_CAPACITY reports.
+fn to_host<F>(n: usize, face_cap: usize, call: F) -> Result<HostResults, Error>
+where
+    F: Fn(*mut f64, *mut u64, *mut u32, *mut i32, *mut f64, usize, *mut usize) -> tess_status,
+{
+    let mut cap = face_cap.max(1);
+    for _ in 0..2 {
+        let nbr = PinnedBuf::<i32>::new(cap)?;
+        let area = PinnedBuf::<f64>::new(cap)?;
+        let mut volumes = vec![0.0f64; n];
+        let mut face_start = vec![0u64; n];
+        let mut face_count = vec![0u32; n];
+        let mut used = 0usize;
+        let st = call(volumes.as_mut_ptr(), face_start.as_mut_ptr(), face_count.as_mut_ptr(), nbr.ptr, area.ptr, cap,
+                      &mut used);
+        if st == TESS_E_CAPACITY {
+            cap = used;
+            continue;
+        }
+        check(st)?;
+        return Ok(HostResults { volumes, face_start, face_count, face_nbr: nbr, face_area: area, faces_used: used });
+    }
+    Err(Error { status: TESS_E_CAPACITY, message: last_error() })
 }
 
 /// Pinned, device-mapped host memory (tess_host_alloc).
@@ -444,6 +451,16 @@ impl Batch {
 
     pub fn compute(&mut self, precision: Precision) -> Result<(), Error> {
         check(unsafe { tess_batch_compute(self.h, precision.code()) })
+    }
+
+    /// `compute` with the faces written into a pinned host pool as the cells
+    /// finish (tess_batch_compute_to_host); neighbour ids are local to each
+    /// diagram.
+    pub fn compute_to_host(&mut self, precision: Precision, face_cap: usize) -> Result<HostResults, Error> {
+        let (h, p) = (self.h, precision.code());
+        to_host(self.n, face_cap, |v, fs, fc, nb, ar, cap, used| unsafe {
+            tess_batch_compute_to_host(h, p, v, fs, fc, nb, ar, cap, used)
+        })
     }
 
     /// As Diagram::autotune, with the batch's grid density among the knobs.

@@ -167,3 +167,57 @@ def test_one_million_cells_properties(T):
     a = src[inner] * len(pts) + nbr[inner]
     b = nbr[inner].astype(np.int64) * len(pts) + src[inner]
     assert np.array_equal(np.sort(a), np.sort(b))
+
+
+def _batch_inputs(sizes, seed):
+    from tessellator import workloads
+
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    pts = np.concatenate([workloads.uniform(s, seed=seed + k) for k, s in enumerate(sizes)])
+    boxes = np.array([[0, 0, 0, 1, 1, 1]] * len(sizes), dtype=np.float64)
+    return pts, offs, boxes
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed"])
+def test_batch_same_results_as_compute(T, prec):
+    pts, offs, boxes = _batch_inputs([64, 3000, 999, 5000, 17, 2048], 60)
+    b = T.Batch(pts, offs, boxes)
+    try:
+        b.compute(prec)
+        vol = b.volumes()
+        co, cn, ca = b.neighbors_csr()
+        pool_a = (T.pinned_empty(20 * len(pts), np.int32), T.pinned_empty(20 * len(pts), np.float64))
+        pool_b = (T.pinned_empty(21 * len(pts), np.int32), T.pinned_empty(21 * len(pts), np.float64))
+        # two pools in turn: each keeps its own captured graph valid
+        for pool in (pool_a, pool_b, pool_a):
+            r = b.compute_to_host(prec, face_pool=pool)
+            assert np.array_equal(r.volumes, vol)
+            o2, n2, a2 = r.csr()
+            assert np.array_equal(o2, co) and np.array_equal(n2, cn) and np.array_equal(a2, ca)
+        with pytest.raises(T.TessError) as e:
+            b.neighbors_csr()
+        assert e.value.status == T._capi.TESS_E_STATE
+        # the library's own pool again
+        b.compute(prec)
+        assert np.array_equal(b.neighbors_csr()[1], cn)
+    finally:
+        b.close()
+
+
+def test_batch_pool_too_small(T):
+    pts, offs, boxes = _batch_inputs([2000, 3000], 70)
+    L = T.lib()
+    b = T.Batch(pts, offs, boxes)
+    try:
+        n = len(pts)
+        small = (T.pinned_empty(500, np.int32), T.pinned_empty(500, np.float64))
+        vol, fs, fc = np.empty(n), np.empty(n, dtype=np.uint64), np.empty(n, dtype=np.uint32)
+        used = C.c_size_t(0)
+        st = L.tess_batch_compute_to_host(b._h, T.PRECISION_FP32_GUARD, vol.ctypes.data, fs.ctypes.data,
+                                          fc.ctypes.data, small[0].ctypes.data, small[1].ctypes.data, 500,
+                                          C.byref(used))
+        assert st == T._capi.TESS_E_CAPACITY and used.value > 500
+        r = b.compute_to_host("fp32")   # allocates, and grows once if needed
+        assert abs(r.volumes[:2000].sum() - 1.0) < 1e-6 and abs(r.volumes[2000:].sum() - 1.0) < 1e-6
+    finally:
+        b.close()

@@ -232,6 +232,13 @@ struct Engine {
     uint64_t launches = 0;    // kernels launched so far (all passes)
     cudaGraphExec_t graph = nullptr;
     int graph_precision = -1;
+    // the batch graph captured with a caller's face pool
+    // (tess_batch_compute_to_host): its pointers, capacity and precision
+    cudaGraphExec_t graph_host = nullptr;
+    int graph_host_precision = -1;
+    const void* graph_host_nbr = nullptr;
+    const void* graph_host_area = nullptr;
+    uint64_t graph_host_cap = 0;
     int blocks_cache[2][4][8] = {};   // [kernel type][slots][form, with the exact flag]
     // allocated capacities of the grid arrays a re-grid may grow
     uint64_t delims_alloc = 0, table_alloc = 0;
@@ -244,9 +251,15 @@ struct Engine {
 
     ~Engine() { release(); }
 
-    void release() {
+    void drop_graphs() {
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
+        if (graph_host) cudaGraphExecDestroy(graph_host);
+        graph_host = nullptr;
+    }
+
+    void release() {
+        drop_graphs();
         dfree(d_xyz); dfree(d_groups); dfree(d_desc); dfree(d_chunk_diag); dfree(d_chunk_start);
         dfree(d_bounds); dfree(d_bin); dfree(d_rank); dfree(d_delims); dfree(d_scan_tmp);
         dfree(d_sorted); dfree(d_inv); dfree(d_spx); dfree(d_spy); dfree(d_spz); dfree(d_shi); dfree(d_slo); dfree(d_sgroup);
@@ -817,8 +830,7 @@ tess_status engine_regrid(Engine& E, double density) {
     E.table_total = tab;
     E.cfg.bin_density = density;
     CU(cudaMemcpyAsync(E.d_desc, E.hdesc.data(), sizeof(DiagDesc) * E.ndiag, cudaMemcpyHostToDevice, E.stream));
-    if (E.graph) cudaGraphExecDestroy(E.graph);
-    E.graph = nullptr;
+    E.drop_graphs();
     return engine_build(E, true);
 }
 
@@ -920,8 +932,7 @@ tess_status time_sample(Engine& E, int precision, uint32_t m, float* ms) {
         TRY(dalloc(&E.d_fnbr, E.face_cap));
         TRY(dalloc(&E.d_farea, E.face_cap));
         E.stats.face_pool_regrows += 1;
-        if (E.graph) cudaGraphExecDestroy(E.graph);
-        E.graph = nullptr;
+        E.drop_graphs();
     }
     return fail(TESS_E_NOMEM, "face pool could not be sized");
 }
@@ -965,8 +976,7 @@ tess_status engine_autotune(Engine& E, int precision, bool batch, const char* ca
         E.cfg.crowded_bin = cached.crowded_bin;
         std::memset(E.blocks_cache, 0, sizeof(E.blocks_cache));
         if (batch && cached.bin_density != E.cfg.bin_density) TRY(engine_regrid(E, cached.bin_density));
-        if (E.graph) cudaGraphExecDestroy(E.graph);
-        E.graph = nullptr;
+        E.drop_graphs();
         cached.from_cache = 1;
         cached.trials = 0;
         cached.max_bin_points = T.max_bin_points;
@@ -1023,8 +1033,7 @@ tess_status engine_autotune(Engine& E, int precision, bool batch, const char* ca
     E.cfg.crowded_bin = bc;
     std::memset(E.blocks_cache, 0, sizeof(E.blocks_cache));
     if (batch && bd != E.cfg.bin_density) TRY(engine_regrid(E, bd));
-    if (E.graph) cudaGraphExecDestroy(E.graph);
-    E.graph = nullptr;
+    E.drop_graphs();
     T.warps_per_block = bw;
     T.crowded_bin = bc;
     T.bin_density = batch ? bd : E.cfg.bin_density;
@@ -1772,22 +1781,26 @@ tess_status tess_batch_create(size_t ndiag, const uint64_t* pt_offsets, const do
     return TESS_OK;
 }
 
-tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
-    if (!b) return fail(TESS_E_INVALID, "batch is NULL");
+// One batch compute: the captured graph (grid build + passes) for this
+// precision and face pool, captured again when either changed.  With a
+// caller's pool (E.pool_fixed) the graph of that pool is kept beside the
+// library's own.
+static tess_status batch_run(tess_batch* b, int prec) {
     Engine& E = b->E;
-    const int prec = (int)precision;
-    if (prec != TESS_PRECISION_FP64 && prec != TESS_PRECISION_FP32_GUARD && prec != TESS_PRECISION_MIXED)
-        return fail(TESS_E_INVALID, "unknown precision %d", prec);
-    CU(cudaSetDevice(E.device));
-    if ((E.cfg.flags & TESS_FLAG_AUTOTUNE) && !E.tuned) TRY(engine_autotune(E, prec, true, nullptr, nullptr));
-    if (!E.graph || E.graph_precision != prec) {
+    const bool host = E.pool_fixed;
+    cudaGraphExec_t& G = host ? E.graph_host : E.graph;
+    int& gprec = host ? E.graph_host_precision : E.graph_precision;
+    const bool stale = !G || gprec != prec ||
+                       (host && (E.graph_host_nbr != E.d_fnbr || E.graph_host_area != E.d_farea ||
+                                 E.graph_host_cap != E.face_cap));
+    if (stale) {
         // warm the per-kernel attributes and occupancy queries outside capture
         for (int pr : {0, 1})
             for (int s : {2, 4, 8})
                 for (int f : {(int)kFormLean, (int)kFormStd, (int)kFormHybrid})
                     for (int x : {0, (int)kFormExact}) E.blocks(pr, s, f | x);
-        if (E.graph) cudaGraphExecDestroy(E.graph);
-        E.graph = nullptr;
+        if (G) cudaGraphExecDestroy(G);
+        G = nullptr;
         cudaGraph_t g = nullptr;
         CU(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
         tess_status st = TESS_OK;
@@ -1800,10 +1813,15 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
             return st;
         }
         if (ee != cudaSuccess) return fail(TESS_E_CUDA, "end capture: %s", cudaGetErrorString(ee));
-        ce = cudaGraphInstantiate(&E.graph, g, 0);
+        ce = cudaGraphInstantiate(&G, g, 0);
         cudaGraphDestroy(g);
         if (ce != cudaSuccess) return fail(TESS_E_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
-        E.graph_precision = prec;
+        gprec = prec;
+        if (host) {
+            E.graph_host_nbr = E.d_fnbr;
+            E.graph_host_area = E.d_farea;
+            E.graph_host_cap = E.face_cap;
+        }
     }
     TimingEvents ev;
     const bool timing = E.cfg.flags & TESS_FLAG_TIMING;
@@ -1811,7 +1829,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
         CU(ev.create(2));
         CU(cudaEventRecord(ev.e[0], E.stream));
     }
-    CU(cudaGraphLaunch(E.graph, E.stream));
+    CU(cudaGraphLaunch(G, E.stream));
     E.launches += kGridLaunches + (prec != TESS_PRECISION_FP64 ? 7 : 3);
     if (timing) CU(cudaEventRecord(ev.e[1], E.stream));
     unsigned long long used = 0;
@@ -1828,6 +1846,12 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
         return fail(TESS_E_INVALID, "input coordinates must be finite");
     }
     if (gerr == 2) return fail(TESS_E_CUDA, "shell table exceeded its capacity");
+    if (used > E.face_cap && host) {
+        // the caller's pool: report the size needed
+        E.pool_need = used;
+        E.computed = false;
+        return fail(TESS_E_CAPACITY, "%llu faces, face_cap %llu", used, (unsigned long long)E.face_cap);
+    }
     if (used > E.face_cap) {
         // grow the pool; the captured graph holds the old pointer
         dfree(E.d_fnbr);
@@ -1838,7 +1862,7 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
         E.stats.face_pool_regrows += 1;
         cudaGraphExecDestroy(E.graph);
         E.graph = nullptr;
-        return tess_batch_compute(b, precision);
+        return batch_run(b, prec);
     }
     E.stats.cells = E.total;
     E.stats.faces = used;
@@ -1853,9 +1877,65 @@ tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
     E.stats.rerun_degenerate = counts[L_REASON + ST_DEGEN];
     E.computed = true;
     E.csr_valid = false;
+    E.faces_on_host = host;
     E.last_precision = prec;
     if (counts[L_FAIL]) return fail(TESS_E_OVERFLOW, "%u cells could not be computed", counts[L_FAIL]);
     return TESS_OK;
+}
+
+static bool known_precision(int prec) {
+    return prec == TESS_PRECISION_FP64 || prec == TESS_PRECISION_FP32_GUARD || prec == TESS_PRECISION_MIXED;
+}
+
+tess_status tess_batch_compute(tess_batch* b, tess_precision precision) {
+    if (!b) return fail(TESS_E_INVALID, "batch is NULL");
+    Engine& E = b->E;
+    const int prec = (int)precision;
+    if (!known_precision(prec)) return fail(TESS_E_INVALID, "unknown precision %d", prec);
+    CU(cudaSetDevice(E.device));
+    if ((E.cfg.flags & TESS_FLAG_AUTOTUNE) && !E.tuned) TRY(engine_autotune(E, prec, true, nullptr, nullptr));
+    return batch_run(b, prec);
+}
+
+tess_status tess_batch_compute_to_host(tess_batch* b, tess_precision precision, double* volumes,
+                                       uint64_t* face_start, uint32_t* face_count, int32_t* face_nbr,
+                                       double* face_area, size_t face_cap, size_t* faces_used) {
+    if (!b) return fail(TESS_E_INVALID, "batch is NULL");
+    if (!volumes || !face_start || !face_count || !face_nbr || !face_area)
+        return fail(TESS_E_INVALID, "NULL output buffer");
+    Engine& E = b->E;
+    const int prec = (int)precision;
+    if (!known_precision(prec)) return fail(TESS_E_INVALID, "unknown precision %d", prec);
+    CU(cudaSetDevice(E.device));
+    void *dn = nullptr, *da = nullptr;
+    TRY(device_address(face_nbr, &dn, "face_nbr"));
+    TRY(device_address(face_area, &da, "face_area"));
+    // a pending autotune times its samples in the library's own pool
+    if ((E.cfg.flags & TESS_FLAG_AUTOTUNE) && !E.tuned) TRY(engine_autotune(E, prec, true, nullptr, nullptr));
+    int32_t* const own_nbr = E.d_fnbr;
+    double* const own_area = E.d_farea;
+    const uint64_t own_cap = E.face_cap;
+    E.d_fnbr = static_cast<int32_t*>(dn);
+    E.d_farea = static_cast<double*>(da);
+    E.face_cap = face_cap;
+    E.pool_fixed = true;
+    E.pool_need = 0;
+    const tess_status st = batch_run(b, prec);
+    E.d_fnbr = own_nbr;
+    E.d_farea = own_area;
+    E.face_cap = own_cap;
+    E.pool_fixed = false;
+    if (faces_used) *faces_used = st == TESS_E_CAPACITY ? E.pool_need : E.stats.faces;
+    if (st != TESS_OK && st != TESS_E_OVERFLOW) {
+        if (st == TESS_E_CAPACITY) E.faces_on_host = false;
+        return st;
+    }
+    const size_t n = E.total;
+    CU(cudaMemcpyAsync(volumes, E.d_vol, sizeof(double) * n, cudaMemcpyDefault, E.stream));
+    CU(cudaMemcpyAsync(face_start, E.d_fstart, sizeof(uint64_t) * n, cudaMemcpyDefault, E.stream));
+    CU(cudaMemcpyAsync(face_count, E.d_nface, sizeof(uint32_t) * n, cudaMemcpyDefault, E.stream));
+    CU(cudaStreamSynchronize(E.stream));
+    return st;
 }
 
 tess_status tess_batch_update_points(tess_batch* b, const double* xyz, int on_device) {

@@ -92,6 +92,32 @@ def pinned_empty(n: int, dtype) -> np.ndarray:
     return np.frombuffer(buf, dtype=dt, count=int(n))
 
 
+def _to_host(call, n: int, face_pool, default_cap: int) -> "HostResults":
+    """Runs call(volumes, face_start, face_count, nbr, area, cap, used_ref) ->
+    status into fresh per-cell arrays and the face pool (allocated when None,
+    and then grown and retried once on TESS_E_CAPACITY)."""
+    vol = np.empty(n, dtype=np.float64)
+    fstart = np.empty(n, dtype=np.uint64)
+    fcount = np.empty(n, dtype=np.uint32)
+    used = C.c_size_t(0)
+    retry = face_pool is None
+    if face_pool is None:
+        face_pool = (pinned_empty(default_cap, np.int32), pinned_empty(default_cap, np.float64))
+    for _ in range(2):
+        nbr, area = face_pool
+        if len(nbr) != len(area) or nbr.dtype != np.int32 or area.dtype != np.float64:
+            raise ValueError("face_pool: two arrays of equal length, int32 and float64")
+        st = call(vol.ctypes.data, fstart.ctypes.data, fcount.ctypes.data, nbr.ctypes.data, area.ctypes.data,
+                  len(nbr), C.byref(used))
+        if st == TESS_E_CAPACITY and retry:   # the size needed is in used
+            face_pool = (pinned_empty(used.value, np.int32), pinned_empty(used.value, np.float64))
+            retry = False
+            continue
+        check(st)
+        break
+    return HostResults(vol, fstart, fcount, face_pool[0], face_pool[1], used.value)
+
+
 class HostResults:
     """Every cell's results from Diagram.compute_all_to_host: cell i's faces
     are face_nbr / face_area[face_start[i] : face_start[i] + face_count[i]]
@@ -254,32 +280,11 @@ class Diagram:
         when the call reports a larger size).  The faces then exist only in
         that pool: neighbors_csr and the per-cell face queries need another
         compute_all."""
-        L = lib()
-        vol = np.empty(self.n, dtype=np.float64)
-        fstart = np.empty(self.n, dtype=np.uint64)
-        fcount = np.empty(self.n, dtype=np.uint32)
-        used = C.c_size_t(0)
-        if face_pool is None:
-            cap = 20 * self.n + 1024
-            face_pool = (pinned_empty(cap, np.int32), pinned_empty(cap, np.float64))
-            retry = True
-        else:
-            retry = False
-        for _ in range(2):
-            nbr, area = face_pool
-            if len(nbr) != len(area) or nbr.dtype != np.int32 or area.dtype != np.float64:
-                raise ValueError("face_pool: two arrays of equal length, int32 and float64")
-            st = L.tess_diagram_compute_all_to_host(
-                self._h, _prec(precision), _radius(search_radius), _group(target_group), vol.ctypes.data,
-                fstart.ctypes.data, fcount.ctypes.data, nbr.ctypes.data, area.ctypes.data, len(nbr),
-                C.byref(used))
-            if st == TESS_E_CAPACITY and retry:   # the size needed is in used
-                face_pool = (pinned_empty(used.value, np.int32), pinned_empty(used.value, np.float64))
-                retry = False
-                continue
-            check(st)
-            break
-        return HostResults(vol, fstart, fcount, face_pool[0], face_pool[1], used.value)
+        def call(*a):
+            return lib().tess_diagram_compute_all_to_host(self._h, _prec(precision), _radius(search_radius),
+                                                          _group(target_group), *a)
+
+        return _to_host(call, self.n, face_pool, 20 * self.n + 1024)
 
     def volumes(self) -> np.ndarray:
         out = np.empty(self.n, dtype=np.float64)
@@ -545,6 +550,15 @@ class Batch:
         Diagram.compute_all), in one CUDA-graph launch per precision."""
         check(lib().tess_batch_compute(self._h, _prec(precision)))
         return self
+
+    def compute_to_host(self, precision="fp32", face_pool=None) -> "HostResults":
+        """compute with the faces written into a pinned host pool as the cells
+        finish (tess_batch_compute_to_host); see Diagram.compute_all_to_host.
+        Neighbour ids are local to each diagram."""
+        def call(*a):
+            return lib().tess_batch_compute_to_host(self._h, _prec(precision), *a)
+
+        return _to_host(call, self.n, face_pool, 20 * self.n + 1024)
 
     def autotune(self, precision="fp32", cache_path: Optional[str] = None) -> dict:
         """As Diagram.autotune, with the batch's grid density among the knobs."""

@@ -39,7 +39,7 @@ EXPORTS = (
     "tess_diagram_compute_all_to_host", "tess_host_alloc", "tess_host_free",
     "tess_find_cells_in_radius", "tess_find_neighbors_in_radius", "tess_neighbor_cloud",
     "tess_neighbor_cloud_at",
-    "tess_batch_create", "tess_batch_compute", "tess_batch_update_points", "tess_batch_stats", "tess_batch_volumes",
+    "tess_batch_create", "tess_batch_compute", "tess_batch_compute_to_host", "tess_batch_update_points", "tess_batch_stats", "tess_batch_volumes",
     "tess_batch_neighbors_csr", "tess_batch_results_device", "tess_batch_destroy",
     "tess_diagram_autotune", "tess_batch_autotune", "tess_csr_offsets_noalloc",
 )
@@ -144,6 +144,7 @@ def lib():
                                         C.c_size_t, szp]),
         "tess_batch_create": (st, [C.c_size_t, u64p, dp, dp, C.POINTER(Config), C.POINTER(vp)]),
         "tess_batch_compute": (st, [vp, C.c_int]),
+        "tess_batch_compute_to_host": (st, [vp, C.c_int, vp, vp, vp, vp, vp, C.c_size_t, szp]),
         "tess_batch_update_points": (st, [vp, vp, C.c_int]),
         "tess_batch_stats": (st, [vp, C.POINTER(Stats)]),
         "tess_batch_volumes": (st, [vp, dp]),
