@@ -97,7 +97,7 @@ struct Smem {
             T px[P], py[P], pz[P], pd[P];     // plane: normal, offset (n.x = offset)
             T pn[P];                          // |normal| (1 for the FP64 form and the walls)
             T vsd[V];                         // signed distances of the current cut
-            T vr[V];                          // (|v| + e_v)^2 of each slot (FP32), |v|^2 (FP64)
+            float vr[V];                      // (|v| + e_v)^2 of each slot (FP32), |v|^2 rounded up (FP64)
             T cbx[32], cby[32], cbz[32], cb2[32];   // kept candidates waiting for a full window ...
             uint32_t cbj[32];                 // ... their sorted indices
             int32_t cbid[32];                 // ... and local original ids
@@ -148,13 +148,6 @@ __device__ __forceinline__ unsigned warp_incl_scan_u(unsigned v, int lane) {
         unsigned t = __shfl_up_sync(FULL, v, o);
         if (lane >= o) v += t;
     }
-    return v;
-}
-
-template <typename T>
-__device__ __forceinline__ T warp_max_t(T v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(FULL, v, o));
     return v;
 }
 
@@ -283,26 +276,41 @@ __device__ __forceinline__ void bisector(float rx, float ry, float rz, float r2,
     off = 0.5f * r2;
     rn = sqrt_up(r2);     // an upper bound: it only widens the guard band
 }
+// FP64 form: unnormalised too, with rn = r.r = |n|^2, so that the
+// reference's test of the normalised signed distance against 1e-12
+// (Plane::vector_location, vector3.rs:170-185) runs on squares (above_tol):
+// no square root and no division per candidate.  A normalised plane cost
+// ~27 FP64-pipe instructions per candidate, and the plain FP64 form is bound
+// by that pipe.
 __device__ __forceinline__ void bisector(double rx, double ry, double rz, double r2, double& nx,
                                          double& ny, double& nz, double& off, double& rn) {
-    rn = 1.0;
-    const double inv = 1.0 / sqrt(r2);
-    nx = rx * inv;
-    ny = ry * inv;
-    nz = rz * inv;
-    off = nx * (rx * 0.5) + ny * (ry * 0.5) + nz * (rz * 0.5);
+    nx = rx;
+    ny = ry;
+    nz = rz;
+    off = 0.5 * r2;
+    rn = r2;
 }
+
+// The FP64 form's tolerance tests for a plane with |n|^2 = n2, tol2 =
+// 1e-24 n2: sd / |n| > 1e-12 (Outside) and sd / |n| < -1e-12 (Inside, not
+// Incident), by squares.
+__device__ __forceinline__ bool above_tol(double sd, double tol2) { return sd > 0.0 && sd * sd > tol2; }
+__device__ __forceinline__ bool below_tol(double sd, double tol2) { return sd < 0.0 && sd * sd > tol2; }
 
 __device__ __forceinline__ float round_up_f(float x) { return x; }
 __device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
 
 // A vertex's share of the cell radius: (|v| + e_v)^2 in the FP32 form (|v|
-// from the upper-bound root), |v|^2 in the FP64 form.
+// from the upper-bound root), |v|^2 rounded up to FP32 in the FP64 form (the
+// radius only bounds the search, and FP32 keeps its warp maximum off the FP64
+// pipe).
 __device__ __forceinline__ float vrad2(float x, float y, float z, float e) {
     const float r = sqrt_up(x * x + y * y + z * z) + e;
     return r * r;
 }
-__device__ __forceinline__ double vrad2(double x, double y, double z, double) { return x * x + y * y + z * z; }
+__device__ __forceinline__ float vrad2(double x, double y, double z, double) {
+    return __double2float_ru(x * x + y * y + z * z);
+}
 
 // Per-warp work counters (reported when ClipParams::work_ctr is set).  The
 // lean first-pass form does not count: the registers cost it 2%.
@@ -497,7 +505,7 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
                 pe += gr * x1;
             } else {
                 const T den = xsd - ysd;
-                const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / den;
+                const T t = !below_tol(ysd, (T)(kTolerance * kTolerance) * rn) ? (T)1 : xsd / den;
                 px = xx + (yx - xx) * t;
                 py = xy + (yy - xy) * t;
                 pz = xz + (yz - xz) * t;
@@ -563,7 +571,7 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
         S.py[f] = ny;
         S.pz[f] = nz;
         S.pd[f] = off;
-        S.pn[f] = rn;
+        S.pn[f] = GUARD ? rn : (T)1;
         S.pid[f] = id;
         S.psrc[f] = src;
     }
@@ -674,6 +682,8 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
     // the plane's share of the test's FP32 rounding (FP32 form)
     const T gr = GUARD ? (T)P.guard_rel : (T)0;
     const T rc = gr * rn;
+    // FP64 form: the tolerance test by squares, rn = |n|^2 (see bisector)
+    const T tol2 = GUARD ? (T)0 : (T)(kTolerance * kTolerance) * rn;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         sd[k] = (T)0;
@@ -684,7 +694,9 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         if (C.lm[k] == 0) continue;
         const bool live = (C.lm[k] >> lane) & 1u;
         sd[k] = sdist(nx, ny, nz, off, C.vx[k], C.vy[k], C.vz[k]);
-        const bool out = live && sd[k] > (GUARD ? (T)0 : (T)kTolerance);
+        bool out;
+        if constexpr (GUARD) out = live && sd[k] > (T)0;
+        else out = live && above_tol(sd[k], tol2);
         if constexpr (GUARD) gh |= live && fabs(sd[k]) <= fma(rn, C.ve[k] + rc, eC);
         om[k] = __ballot_sync(FULL, out);
     }
@@ -805,7 +817,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             } else {
                 const T xx = S.vx[x], xy = S.vy[x], xz = S.vz[x], xsd = S.vsd[x];
                 const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
-                const T t = ysd >= -(T)kTolerance ? (T)1 : xsd / (xsd - ysd);
+                const T t = !below_tol(ysd, tol2) ? (T)1 : xsd / (xsd - ysd);
                 px = xx + (yx - xx) * t;
                 py = xy + (yy - xy) * t;
                 pz = xz + (yz - xz) * t;
@@ -862,7 +874,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             S.py[f] = ny;
             S.pz[f] = nz;
             S.pd[f] = off;
-            S.pn[f] = rn;
+            S.pn[f] = GUARD ? rn : (T)1;
             S.pid[f] = id;
             S.psrc[f] = src;
         }
@@ -880,25 +892,22 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
     return cut_general<T, K, GUARD, RESOLVE>(S, C, sdv, omv, nx, ny, nz, off, rn, cR, gr, id, src, f, lane, P.check);
 }
 
-// Squared radius of the cell about its site: max |v|^2 over live vertices;
-// in the FP32 form each |v| is inflated by its error bound.  Each slot's term
-// (vrad2) is written with the vertex, so a cut costs one load per register
-// set here instead of a square root per vertex.
+// Squared radius of the cell about its site: max |v|^2 over live vertices,
+// an upper bound (FP32 form: each |v| inflated by its error bound; FP64
+// form: |v|^2 rounded up to FP32).  Each slot's term (vrad2) is written with
+// the vertex, so a cut costs one load per register set here instead of a
+// square root per vertex.
 template <typename T, int K>
 __device__ __forceinline__ T live_r2(const Smem<T, K>& S, const CellRegs<T, K>& C, int lane) {
-    T r2 = 0;
+    float r2 = 0.f;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         if (C.lm[k] == 0) continue;
-        if ((C.lm[k] >> lane) & 1u) r2 = max(r2, S.vr[k * 32 + lane]);
+        if ((C.lm[k] >> lane) & 1u) r2 = fmaxf(r2, S.vr[k * 32 + lane]);
     }
-    if constexpr (sizeof(T) == 4) {
-        // r2 >= 0 and never NaN (max drops NaN): its bits order like its
-        // value, so one warp reduction of the bits gives the maximum
-        return __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(r2)));
-    } else {
-        return warp_max_t(r2);
-    }
+    // r2 >= 0 and never NaN (fmaxf drops NaN): its bits order like its
+    // value, so one warp reduction of the bits gives the maximum
+    return (T)__uint_as_float(__reduce_max_sync(FULL, __float_as_uint(r2)));
 }
 
 __device__ __forceinline__ void ring_offset(int s, uint32_t r, int& i, int& j, int& k) {
@@ -1055,7 +1064,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     __syncwarp();
     T R2 = live_r2(S, C, lane);
     // guard_rel * cell radius: the hybrid form's limit on a vertex's error bound
-    T cR = (T)P.guard_rel * sqrt_up(R2);
+    T cR = GUARD ? (T)P.guard_rel * sqrt_up(R2) : (T)0;
     // FP32 form, the hi/lo split's share of a plane test's error (u = 2^-24,
     // positions relative to the diagram's centre): per component the offset
     // r~ = (hi_p - hi_s) + (lo_p - lo_s) is off by at most 2u |r| (relative,
@@ -1129,7 +1138,8 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                         const int sl = k * 32 + __ffs(m) - 1;
                         m &= m - 1u;
                         const T sd = sdist(nx_, ny_, nz_, off_, S.vx[sl], S.vy[sl], S.vz[sl]);
-                        out |= sd > (GUARD ? (T)0 : (T)kTolerance);
+                        if constexpr (GUARD) out |= sd > (T)0;
+                        else out |= above_tol(sd, (T)(kTolerance * kTolerance) * rn_);
                         if constexpr (GUARD) amb |= fabs(sd) <= fma(rn_, S.ve[sl] + (T)P.guard_rel * rn_, eC);
                     }
                 }
@@ -1172,7 +1182,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 }
                 const T R2b = R2;
                 R2 = live_r2(S, C, lane);
-                cR = (T)P.guard_rel * sqrt_up(R2);
+                if constexpr (GUARD) cR = (T)P.guard_rel * sqrt_up(R2);
                 // hybrid form: a cut never moves a vertex beyond the cell
                 // (convexity), so a radius that grew (or is no longer
                 // finite) means an FP32 vertex went wrong after an
