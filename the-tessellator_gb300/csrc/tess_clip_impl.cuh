@@ -83,6 +83,7 @@ struct Smem {
     static constexpr int VUSE = V < 255 ? V : 255;                    // slot 255 is the map sentinel
     static constexpr int PF = sizeof(T) == 4 ? P : 1;
     static constexpr int VF = sizeof(T) == 4 ? V : 1;
+    static constexpr int VD = sizeof(T) == 8 ? V : 1;
     // live through the whole cell
     T vx[V], vy[V], vz[V];            // vertex mirror
     int32_t pid[P];                   // neighbour id (local original index) or wall code
@@ -117,6 +118,7 @@ struct Smem {
             // new-vertex ring maps: gen << 8 | slot; entries with another
             // cut's tag are stale
             uint16_t mapf[P], maps[P];
+            float fvx[VD], fvy[VD], fvz[VD];  // FP64 form: the vertices rounded to FP32 (window pre-test)
         };
         struct {                      // finalize
             // FP32 forms only: face planes {n, h} (n.x = h), their distance
@@ -520,6 +522,11 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
             S.vz[slot] = pz;
             if constexpr (GUARD) S.ve[slot] = pe;
             S.vr[slot] = vrad2(px, py, pz, pe);
+            if constexpr (sizeof(T) == 8) {
+                S.fvx[slot % S_t::VD] = (float)px;
+                S.fvy[slot % S_t::VD] = (float)py;
+                S.fvz[slot % S_t::VD] = (float)pz;
+            }
             S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
             // Y's pointer back to X is the edge (b, a) of Y's triple.
             const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
@@ -833,6 +840,11 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             S.vz[slot] = pz;
             if constexpr (GUARD) S.ve[slot] = pe;
             S.vr[slot] = vrad2(px, py, pz, pe);
+            if constexpr (sizeof(T) == 8) {
+                S.fvx[slot % S_t::VD] = (float)px;
+                S.fvy[slot % S_t::VD] = (float)py;
+                S.fvz[slot % S_t::VD] = (float)pz;
+            }
             S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
             // Y's pointer back to X is the edge (b, a) of Y's triple.
             const int yi = (plane_of(ty, 0) == b && plane_of(ty, 1) == a)   ? 0
@@ -1038,6 +1050,11 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         S.vx[lane] = C.vx[0];
         S.vy[lane] = C.vy[0];
         S.vz[lane] = C.vz[0];
+        if constexpr (sizeof(T) == 8) {
+            S.fvx[lane % S_t::VD] = (float)C.vx[0];
+            S.fvy[lane % S_t::VD] = (float)C.vy[0];
+            S.fvz[lane % S_t::VD] = (float)C.vz[0];
+        }
         if constexpr (GUARD) {
             // the corner's rounding to FP32: 2^-24 relative per component from
             // FP64, 2^-23 from the FP32 pairs (doubled here)
@@ -1127,7 +1144,28 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         // the serial nearest-first loop.  Same arithmetic as cut().
         if (BASE != kFormLean && __popc(km) >= kPretestMin) {
             bool maycut = false;
-            if (keep) {
+            if (keep && sizeof(T) == 8) {
+                // FP64 form: the test in FP32 on the vertices' FP32 copies,
+                // kept unless the FP32 distance is below minus four times
+                // its error bound (inputs rounded: 2u |r_i v_i|; FMA chain
+                // and offset: 3u (sum |r_i v_i| + off) + u off; |v_i| <= R)
+                const float fx = (float)rx, fy = (float)ry, fz = (float)rz, f2 = (float)r2;
+                const float Rf = sqrtf((float)R2) * 1.0001f;
+                const float margin = 2.4e-7f * (5.f * (fabsf(fx) + fabsf(fy) + fabsf(fz)) * Rf + 2.f * f2);
+                const float foff = 0.5f * f2;
+                bool out = false;
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    uint32_t m = C.lm[k];
+                    while (m) {
+                        const int sl = (k * 32 + __ffs(m) - 1) % S_t::VD;
+                        m &= m - 1u;
+                        const float sdf = fmaf(fx, S.fvx[sl], fmaf(fy, S.fvy[sl], fmaf(fz, S.fvz[sl], -foff)));
+                        out |= !(sdf <= -margin);
+                    }
+                }
+                maycut = out;
+            } else if (keep) {
                 T nx_, ny_, nz_, off_, rn_;
                 bisector(rx, ry, rz, r2, nx_, ny_, nz_, off_, rn_);
                 bool out = false, amb = false;
@@ -1138,8 +1176,9 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                         const int sl = k * 32 + __ffs(m) - 1;
                         m &= m - 1u;
                         const T sd = sdist(nx_, ny_, nz_, off_, S.vx[sl], S.vy[sl], S.vz[sl]);
-                        if constexpr (GUARD) out |= sd > (T)0;
-                        else out |= above_tol(sd, (T)(kTolerance * kTolerance) * rn_);
+                        // any vertex beyond the plane may be cut (the serial
+                        // test applies the FP64 form's tolerance)
+                        out |= sd > (T)0;
                         if constexpr (GUARD) amb |= fabs(sd) <= fma(rn_, S.ve[sl] + (T)P.guard_rel * rn_, eC);
                     }
                 }
