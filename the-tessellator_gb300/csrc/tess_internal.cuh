@@ -195,6 +195,9 @@ cudaError_t launch_grid_build(const GridBuffers& g, cudaStream_t s, cudaStream_t
                               cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 // inv[sorted[s]] = s for s < n (the point -> sorted position map, on demand).
 cudaError_t launch_inverse(const uint32_t* sorted, uint32_t* inv, uint32_t n, int* check, cudaStream_t s);
+// n bytes from src to dst by the SMs (16-byte aligned pointers; either may be
+// the device address of pinned host memory).
+cudaError_t launch_copy_bytes(void* dst, const void* src, size_t n, int sms, cudaStream_t s);
 // out[0] = most points in one bin, out[1] = points in bins of >= crowd points
 // (every bin of every diagram of the set)
 cudaError_t launch_occupancy(const uint32_t* delims, uint64_t nbins, uint32_t crowd, unsigned long long* out,
