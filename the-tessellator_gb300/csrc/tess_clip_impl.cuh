@@ -922,6 +922,18 @@ __device__ __forceinline__ T live_r2(const Smem<T, K>& S, const CellRegs<T, K>& 
     return (T)__uint_as_float(__reduce_max_sync(FULL, __float_as_uint(r2)));
 }
 
+// The same maximum as an FP32 value (the FP64 form's search bounds).
+template <typename T, int K>
+__device__ __forceinline__ float live_r2f(const Smem<T, K>& S, const CellRegs<T, K>& C, int lane) {
+    float r2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if (C.lm[k] == 0) continue;
+        if ((C.lm[k] >> lane) & 1u) r2 = fmaxf(r2, S.vr[k * 32 + lane]);
+    }
+    return __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(r2)));
+}
+
 __device__ __forceinline__ void ring_offset(int s, uint32_t r, int& i, int& j, int& k) {
     const uint32_t a = 2u * s + 1u, b = 2u * s - 1u;
     const uint32_t nx = 2u * a * a, ny = 2u * b * a;
@@ -1079,7 +1091,17 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
     C.nfree = S_t::VUSE - 8;
     for (int i = lane; i < C.nfree; i += 32) S.fl[i] = (uint8_t)(S_t::VUSE - 1 - i);
     __syncwarp();
-    T R2 = live_r2(S, C, lane);
+    T R2;
+    // FP64 form: the same value in FP32 (R2 is an FP32 upper bound in every
+    // form), for the search bounds, so that they stay off the FP64 pipe;
+    // 4 R2f is then exactly the round_up_f(4 R2) of the other forms
+    float R2f = 0.f;
+    if constexpr (sizeof(T) == 8) {
+        R2f = live_r2f(S, C, lane);
+        R2 = (T)R2f;
+    } else {
+        R2 = live_r2(S, C, lane);
+    }
     // guard_rel * cell radius: the hybrid form's limit on a vertex's error bound
     T cR = GUARD ? (T)P.guard_rel * sqrt_up(R2) : (T)0;
     // FP32 form, the hi/lo split's share of a plane test's error (u = 2^-24,
@@ -1202,11 +1224,22 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             const T c2 = __shfl_sync(FULL, r2, src);
             const uint32_t cj = __shfl_sync(FULL, j, src);
             const int32_t cidb = __shfl_sync(FULL, cid, src);
-            const T lim2 = (T)4 * R2 * (T)kStopMargin;
-            if (!(c2 < lim2)) {
-                // taken in increasing distance: the rest are farther still
-                if (c2 > lim2 * (T)1.001) km = 0;
-                continue;
+            if constexpr (sizeof(T) == 8) {
+                // FP64 form: on the FP32 key (r2 rounded to FP32, truncated)
+                // against the FP32 bound (margin 1e-5); a candidate beyond
+                // reach that passes only costs a test (the cut decides exactly)
+                const float k2 = __uint_as_float(best & ~31u), l2 = 4.f * R2f * (float)kStopMargin;
+                if (!(k2 < l2)) {
+                    if (k2 > l2 * 1.001f) km = 0;
+                    continue;
+                }
+            } else {
+                const T lim2 = (T)4 * R2 * (T)kStopMargin;
+                if (!(c2 < lim2)) {
+                    // taken in increasing distance: the rest are farther still
+                    if (c2 > lim2 * (T)1.001) km = 0;
+                    continue;
+                }
             }
             T nx, ny, nz, off, rn;
             bisector(cx, cy, cz, c2, nx, ny, nz, off, rn);
@@ -1220,7 +1253,12 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                     W.newv += (unsigned)(r - 1);
                 }
                 const T R2b = R2;
-                R2 = live_r2(S, C, lane);
+                if constexpr (sizeof(T) == 8) {
+                    R2f = live_r2f(S, C, lane);
+                    R2 = (T)R2f;
+                } else {
+                    R2 = live_r2(S, C, lane);
+                }
                 if constexpr (GUARD) cR = (T)P.guard_rel * sqrt_up(R2);
                 // hybrid form: a cut never moves a vertex beyond the cell
                 // (convexity), so a radius that grew (or is no longer
@@ -1279,7 +1317,8 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 if (c < total) {
                     j = tess_chk(bbeg + (c - bpref), P.npts, P.check, CK_POINT);
                     cand(j, rx, ry, rz, r2);
-                    keep = (j != self) && r2 > dup2 && r2 < lim;
+                    if constexpr (sizeof(T) == 8) keep = (j != self) && r2 > dup2 && (float)r2 < 4.f * R2f * (float)kStopMargin;
+                    else keep = (j != self) && r2 > dup2 && r2 < lim;
                     if constexpr (GUARD) near = (j != self) && !(r2 > dup2);
                     if constexpr (kSeedForm) keep = keep && j != seedj;
                     cid = (int32_t)(P.sorted[j] - pt_base);
@@ -1372,7 +1411,7 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
         const int x = cbx + i, y = cby + j, z = cbz + k;
         if (x < 0 || x >= cpd || y < 0 || y >= cpd || z < 0 || z >= cpd) return -1;
         // no point of this bin can cut: it lies beyond twice the cell radius
-        if (near_ok && near2(i, j, k) * (1.0f - 1e-4f) >= round_up_f((T)4 * R2))
+        if (near_ok && near2(i, j, k) * (1.0f - 1e-4f) >= (sizeof(T) == 8 ? 4.f * R2f : round_up_f((T)4 * R2)))
             return -1;
         return (long long)tess_chk(bin_base + ((uint64_t)x * cpd + y) * cpd + z, P.nbins, P.check, CK_BIN);
     };
@@ -1530,7 +1569,8 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
                 S.pending = pending & ~(1u << cbin);
                 S.cbin = cbin;
                 // still within reach of the (shrinking) cell?
-                if (cbin != 13 && S.nd[cbin] * (1.0f - 1e-4f) >= round_up_f((T)4 * R2)) continue;
+                if (cbin != 13 && S.nd[cbin] * (1.0f - 1e-4f) >= (sizeof(T) == 8 ? 4.f * R2f : round_up_f((T)4 * R2)))
+                    continue;
                 const unsigned sbeg = S.nbeg[cbin], scnt = S.ncnt[cbin];
                 T drx = 0, dry = 0, drz = 0, dr2 = (T)INFINITY;
                 seedj = 0xFFFFFFFFu;
@@ -1575,13 +1615,15 @@ __device__ void run_cell(const ClipParams& P, Smem<T, K>& S, uint32_t gs, int la
             }
             // The table key is rounded toward zero and the threshold up, so
             // stopping on key >= thr never drops a bin that could hold a cutter.
-            const float thr = round_up_f((T)4 * R2 * (T)kStopMargin);
+            const float thr = sizeof(T) == 8 ? 4.f * R2f * (float)kStopMargin : round_up_f((T)4 * R2 * (T)kStopMargin);
             const unsigned ma = __ballot_sync(FULL, !(ea.key < thr));
             const int na = ma ? __ffs(ma) - 1 : 32;
             ba = ea.beg;
             ca = lane < na ? ea.cnt : 0u;
             // re-test the bins against the current (smaller) radius
-            if (ca && near_ok && near2(ea.i, ea.j, ea.k) * (1.0f - 1e-4f) >= round_up_f((T)4 * R2)) ca = 0;
+            if (ca && near_ok &&
+                near2(ea.i, ea.j, ea.k) * (1.0f - 1e-4f) >= (sizeof(T) == 8 ? 4.f * R2f : round_up_f((T)4 * R2)))
+                ca = 0;
             t += (uint32_t)na;
             if (ma) {
                 ph = (t >= tab_len) && isfinite(D.tab_kmax) ? 2 : 3;
