@@ -521,11 +521,18 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
             S.vy[slot] = py;
             S.vz[slot] = pz;
             if constexpr (GUARD) S.ve[slot] = pe;
-            S.vr[slot] = vrad2(px, py, pz, pe);
             if constexpr (sizeof(T) == 8) {
-                S.fvx[slot % S_t::VD] = (float)px;
-                S.fvy[slot % S_t::VD] = (float)py;
-                S.fvz[slot % S_t::VD] = (float)pz;
+                // FP64 form: the FP32 copies (rounded to nearest) serve the
+                // window pre-test and the cell radius: |v|^2 from them, times
+                // 1 + 5 * 2^-23 (the copies' and the sum's rounding are at
+                // most 2.5 * 2^-23), is an upper bound, off the FP64 pipe
+                const float fx = (float)px, fy = (float)py, fz = (float)pz;
+                S.fvx[slot % S_t::VD] = fx;
+                S.fvy[slot % S_t::VD] = fy;
+                S.fvz[slot % S_t::VD] = fz;
+                S.vr[slot] = fmaf(fx, fx, fmaf(fy, fy, fz * fz)) * 1.000000596f;
+            } else {
+                S.vr[slot] = vrad2(px, py, pz, pe);
             }
             S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
             // Y's pointer back to X is the edge (b, a) of Y's triple.
@@ -839,11 +846,18 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             S.vy[slot] = py;
             S.vz[slot] = pz;
             if constexpr (GUARD) S.ve[slot] = pe;
-            S.vr[slot] = vrad2(px, py, pz, pe);
             if constexpr (sizeof(T) == 8) {
-                S.fvx[slot % S_t::VD] = (float)px;
-                S.fvy[slot % S_t::VD] = (float)py;
-                S.fvz[slot % S_t::VD] = (float)pz;
+                // FP64 form: the FP32 copies (rounded to nearest) serve the
+                // window pre-test and the cell radius: |v|^2 from them, times
+                // 1 + 5 * 2^-23 (the copies' and the sum's rounding are at
+                // most 2.5 * 2^-23), is an upper bound, off the FP64 pipe
+                const float fx = (float)px, fy = (float)py, fz = (float)pz;
+                S.fvx[slot % S_t::VD] = fx;
+                S.fvy[slot % S_t::VD] = fy;
+                S.fvz[slot % S_t::VD] = fz;
+                S.vr[slot] = fmaf(fx, fx, fmaf(fy, fy, fz * fz)) * 1.000000596f;
+            } else {
+                S.vr[slot] = vrad2(px, py, pz, pe);
             }
             S.tri[slot] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)f << 16);
             // Y's pointer back to X is the edge (b, a) of Y's triple.
