@@ -280,8 +280,8 @@ __device__ __forceinline__ void bisector(float rx, float ry, float rz, float r2,
 }
 // FP64 form: unnormalised too, with rn = r.r = |n|^2, so that the
 // reference's test of the normalised signed distance against 1e-12
-// (Plane::vector_location, vector3.rs:170-185) runs on squares (above_tol):
-// no square root and no division per candidate.  A normalised plane cost
+// (Plane::vector_location, vector3.rs:170-185) compares with one threshold
+// (tol_of): no FP64 square root and no division per candidate.  A normalised plane cost
 // ~27 FP64-pipe instructions per candidate, and the plain FP64 form is bound
 // by that pipe.
 __device__ __forceinline__ void bisector(double rx, double ry, double rz, double r2, double& nx,
@@ -293,11 +293,15 @@ __device__ __forceinline__ void bisector(double rx, double ry, double rz, double
     rn = r2;
 }
 
-// The FP64 form's tolerance tests for a plane with |n|^2 = n2, tol2 =
-// 1e-24 n2: sd / |n| > 1e-12 (Outside) and sd / |n| < -1e-12 (Inside, not
-// Incident), by squares.
-__device__ __forceinline__ bool above_tol(double sd, double tol2) { return sd > 0.0 && sd * sd > tol2; }
-__device__ __forceinline__ bool below_tol(double sd, double tol2) { return sd < 0.0 && sd * sd > tol2; }
+// The FP64 form's tolerance for a plane with |n|^2 = n2: Outside is
+// sd > 1e-12 |n|, Inside sd < -1e-12 |n| (the reference's test on the
+// normalised distance).  |n| comes from the FP32 square root: off by ~1e-7 of
+// 1e-12 |n|, far inside the FP64 rounding of a signed distance, and each test
+// is one compare.  Planes beyond FP32's range take the FP64 root.
+__device__ __forceinline__ double tol_of(double n2) {
+    const float n2f = (float)n2;
+    return n2f < 1e37f ? (double)(1e-12f * sqrtf(n2f)) : kTolerance * sqrt(n2);
+}
 
 __device__ __forceinline__ float round_up_f(float x) { return x; }
 __device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
@@ -507,7 +511,7 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
                 pe += gr * x1;
             } else {
                 const T den = xsd - ysd;
-                const T t = !below_tol(ysd, (T)(kTolerance * kTolerance) * rn) ? (T)1 : xsd / den;
+                const T t = ysd >= -(T)tol_of(rn) ? (T)1 : xsd / den;
                 px = xx + (yx - xx) * t;
                 py = xy + (yy - xy) * t;
                 pz = xz + (yz - xz) * t;
@@ -696,8 +700,9 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
     // the plane's share of the test's FP32 rounding (FP32 form)
     const T gr = GUARD ? (T)P.guard_rel : (T)0;
     const T rc = gr * rn;
-    // FP64 form: the tolerance test by squares, rn = |n|^2 (see bisector)
-    const T tol2 = GUARD ? (T)0 : (T)(kTolerance * kTolerance) * rn;
+    // FP64 form: the tolerance of the normalised test, rn = |n|^2 (see bisector)
+    T tolr = 0;
+    if constexpr (!GUARD) tolr = tol_of(rn);
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         sd[k] = (T)0;
@@ -710,7 +715,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
         sd[k] = sdist(nx, ny, nz, off, C.vx[k], C.vy[k], C.vz[k]);
         bool out;
         if constexpr (GUARD) out = live && sd[k] > (T)0;
-        else out = live && above_tol(sd[k], tol2);
+        else out = live && sd[k] > tolr;
         if constexpr (GUARD) gh |= live && fabs(sd[k]) <= fma(rn, C.ve[k] + rc, eC);
         om[k] = __ballot_sync(FULL, out);
     }
@@ -831,7 +836,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             } else {
                 const T xx = S.vx[x], xy = S.vy[x], xz = S.vz[x], xsd = S.vsd[x];
                 const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
-                const T t = !below_tol(ysd, tol2) ? (T)1 : xsd / (xsd - ysd);
+                const T t = ysd >= -tolr ? (T)1 : xsd / (xsd - ysd);
                 px = xx + (yx - xx) * t;
                 py = xy + (yy - xy) * t;
                 pz = xz + (yz - xz) * t;
