@@ -298,6 +298,21 @@ __device__ __forceinline__ void bisector(double rx, double ry, double rz, double
 // normalised distance).  |n| comes from the FP32 square root: off by ~1e-7 of
 // 1e-12 |n|, far inside the FP64 rounding of a signed distance, and each test
 // is one compare.  Planes beyond FP32's range take the FP64 root.
+// 1/d for the FP64 form's edge interpolation, by Newton-Raphson: the FP32
+// reciprocal, then two steps y' = y + y (1 - d y) in FP64, each of which
+// squares the relative error (2^-23 -> 2^-46 -> the FP64 rounding, about 2
+// ulp in all).  Outside FP32's normal range, the FP64 division.
+__device__ __forceinline__ double recip_nr(double d) {
+    const float df = (float)d;
+    const float a = fabsf(df);
+    if (!(a > 1e-36f && a < 1e36f)) return 1.0 / d;
+    double y = (double)__frcp_rn(df);
+    double e = fma(-d, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-d, y, 1.0);
+    return fma(y, e, y);
+}
+
 __device__ __forceinline__ double tol_of(double n2) {
     const float n2f = (float)n2;
     return n2f < 1e37f ? (double)(1e-12f * sqrtf(n2f)) : kTolerance * sqrt(n2);
@@ -511,7 +526,7 @@ __device__ __forceinline__ int cut_general(Smem<T, K>& S, CellRegs<T, K>& C, con
                 pe += gr * x1;
             } else {
                 const T den = xsd - ysd;
-                const T t = ysd >= -(T)tol_of(rn) ? (T)1 : xsd / den;
+                const T t = ysd >= -(T)tol_of(rn) ? (T)1 : xsd * recip_nr(den);
                 px = xx + (yx - xx) * t;
                 py = xy + (yy - xy) * t;
                 pz = xz + (yz - xz) * t;
@@ -836,7 +851,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
             } else {
                 const T xx = S.vx[x], xy = S.vy[x], xz = S.vz[x], xsd = S.vsd[x];
                 const T yx = S.vx[y], yy = S.vy[y], yz = S.vz[y], ysd = S.vsd[y];
-                const T t = ysd >= -tolr ? (T)1 : xsd / (xsd - ysd);
+                const T t = ysd >= -tolr ? (T)1 : xsd * recip_nr(xsd - ysd);
                 px = xx + (yx - xx) * t;
                 py = xy + (yy - xy) * t;
                 pz = xz + (yz - xz) * t;
