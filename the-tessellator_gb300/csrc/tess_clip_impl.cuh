@@ -281,9 +281,9 @@ __device__ __forceinline__ void bisector(float rx, float ry, float rz, float r2,
 // FP64 form: unnormalised too, with rn = r.r = |n|^2, so that the
 // reference's test of the normalised signed distance against 1e-12
 // (Plane::vector_location, vector3.rs:170-185) compares with one threshold
-// (tol_of): no FP64 square root and no division per candidate.  A normalised plane cost
-// ~27 FP64-pipe instructions per candidate, and the plain FP64 form is bound
-// by that pipe.
+// (tol_of): no FP64 square root and no division per candidate.  A normalised
+// plane cost ~27 FP64-pipe instructions per candidate, and the plain FP64 form
+// is bound by that pipe.
 __device__ __forceinline__ void bisector(double rx, double ry, double rz, double r2, double& nx,
                                          double& ny, double& nz, double& off, double& rn) {
     nx = rx;
@@ -293,11 +293,6 @@ __device__ __forceinline__ void bisector(double rx, double ry, double rz, double
     rn = r2;
 }
 
-// The FP64 form's tolerance for a plane with |n|^2 = n2: Outside is
-// sd > 1e-12 |n|, Inside sd < -1e-12 |n| (the reference's test on the
-// normalised distance).  |n| comes from the FP32 square root: off by ~1e-7 of
-// 1e-12 |n|, far inside the FP64 rounding of a signed distance, and each test
-// is one compare.  Planes beyond FP32's range take the FP64 root.
 // 1/d for the FP64 form's edge interpolation, by Newton-Raphson: the FP32
 // reciprocal, then two steps y' = y + y (1 - d y) in FP64, each of which
 // squares the relative error (2^-23 -> 2^-46 -> the FP64 rounding, about 2
@@ -313,6 +308,11 @@ __device__ __forceinline__ double recip_nr(double d) {
     return fma(y, e, y);
 }
 
+// The FP64 form's tolerance for a plane with |n|^2 = n2: Outside is
+// sd > 1e-12 |n|, Inside sd < -1e-12 |n| (the reference's test on the
+// normalised distance).  |n| comes from the FP32 square root: off by ~1e-7 of
+// 1e-12 |n|, far inside the FP64 rounding of a signed distance, and each test
+// is one compare.  Planes beyond FP32's range take the FP64 root.
 __device__ __forceinline__ double tol_of(double n2) {
     const float n2f = (float)n2;
     return n2f < 1e37f ? (double)(1e-12f * sqrtf(n2f)) : kTolerance * sqrt(n2);
@@ -940,7 +940,7 @@ __device__ int cut(Smem<T, K>& S, CellRegs<T, K>& C, T nx, T ny, T nz, T off, T 
 
 // Squared radius of the cell about its site: max |v|^2 over live vertices,
 // an upper bound (FP32 form: each |v| inflated by its error bound; FP64
-// form: |v|^2 rounded up to FP32).  Each slot's term (vrad2) is written with
+// form: an FP32 upper bound of each |v|^2).  Each slot's term (vrad2) is written with
 // the vertex, so a cut costs one load per register set here instead of a
 // square root per vertex.
 template <typename T, int K>
