@@ -512,15 +512,20 @@ tess_status check_word(Engine& E) {
     return TESS_OK;
 }
 
-// The device address of p when the SMs can reach it (pinned host, device or
-// managed memory), else false (pageable host memory).
-static bool sm_address(const void* p, const void** out) {
+// The address at which kernels on `device` (the current device) may read and
+// write p: pinned host memory (its device mapping), managed memory, or
+// memory of that device.  Pageable host memory and another device's memory
+// have none here (those go through cudaMemcpyAsync).
+static bool sm_address(const void* p, int device, const void** out) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    if (a.type == cudaMemoryTypeUnregistered || !a.devicePointer) return false;
+    if (!a.devicePointer) return false;
+    const bool ok = a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged ||
+                    (a.type == cudaMemoryTypeDevice && a.device == device);
+    if (!ok) return false;
     *out = a.devicePointer;
     return true;
 }
@@ -535,7 +540,7 @@ static bool sm_address(const void* p, const void** out) {
 static tess_status copy_async(Engine& E, void* dst, const void* src, size_t n) {
     if (n == 0) return TESS_OK;
     const void *dd = nullptr, *sd = nullptr;
-    if (sm_address(dst, &dd) && sm_address(src, &sd) && !((reinterpret_cast<uintptr_t>(dd) |
+    if (sm_address(dst, E.device, &dd) && sm_address(src, E.device, &sd) && !((reinterpret_cast<uintptr_t>(dd) |
                                                             reinterpret_cast<uintptr_t>(sd)) & 15u)) {
         if (!E.sm_count) CU(cudaDeviceGetAttribute(&E.sm_count, cudaDevAttrMultiProcessorCount, E.device));
         CU(launch_copy_bytes(const_cast<void*>(dd), sd, n, E.sm_count, E.stream));
@@ -1442,17 +1447,14 @@ tess_status tess_diagram_compute_all(tess_diagram* d, tess_precision precision, 
     return engine_compute(d->E, (int)precision, search_radius, target_group);
 }
 
-// The device address of a buffer the kernels may write: pinned host memory
-// (cudaHostAlloc, cudaHostRegister, tess_host_alloc), device or managed
-// memory.  Pageable host memory has none.
-static tess_status device_address(void* p, void** out, const char* what) {
-    cudaPointerAttributes a{};
-    const cudaError_t e = cudaPointerGetAttributes(&a, p);
-    if (e != cudaSuccess || a.type == cudaMemoryTypeUnregistered || !a.devicePointer) {
-        cudaGetLastError();
-        return fail(TESS_E_INVALID, "%s is not pinned host, device or managed memory", what);
-    }
-    *out = a.devicePointer;
+// The address at which the clipping kernels may write a caller's face pool:
+// pinned host memory (cudaHostAlloc, cudaHostRegister, tess_host_alloc),
+// managed memory, or memory of the handle's device.
+static tess_status device_address(void* p, int device, void** out, const char* what) {
+    const void* a = nullptr;
+    if (!sm_address(p, device, &a))
+        return fail(TESS_E_INVALID, "%s is not pinned host or managed memory, or memory of device %d", what, device);
+    *out = const_cast<void*>(a);
     return TESS_OK;
 }
 
@@ -1466,8 +1468,8 @@ tess_status tess_diagram_compute_all_to_host(tess_diagram* d, tess_precision pre
     Engine& E = d->E;
     CU(cudaSetDevice(E.device));
     void *dn = nullptr, *da = nullptr;
-    TRY(device_address(face_nbr, &dn, "face_nbr"));
-    TRY(device_address(face_area, &da, "face_area"));
+    TRY(device_address(face_nbr, E.device, &dn, "face_nbr"));
+    TRY(device_address(face_area, E.device, &da, "face_area"));
     // a pending autotune times its samples in the library's own pool
     if (E.built && (E.cfg.flags & TESS_FLAG_AUTOTUNE) && !E.tuned &&
         (precision == TESS_PRECISION_FP64 || precision == TESS_PRECISION_FP32_GUARD ||
@@ -1940,8 +1942,8 @@ tess_status tess_batch_compute_to_host(tess_batch* b, tess_precision precision, 
     if (!known_precision(prec)) return fail(TESS_E_INVALID, "unknown precision %d", prec);
     CU(cudaSetDevice(E.device));
     void *dn = nullptr, *da = nullptr;
-    TRY(device_address(face_nbr, &dn, "face_nbr"));
-    TRY(device_address(face_area, &da, "face_area"));
+    TRY(device_address(face_nbr, E.device, &dn, "face_nbr"));
+    TRY(device_address(face_area, E.device, &da, "face_area"));
     // a pending autotune times its samples in the library's own pool
     if ((E.cfg.flags & TESS_FLAG_AUTOTUNE) && !E.tuned) TRY(engine_autotune(E, prec, true, nullptr, nullptr));
     int32_t* const own_nbr = E.d_fnbr;
