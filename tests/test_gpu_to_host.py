@@ -221,3 +221,48 @@ def test_batch_pool_too_small(T):
         assert abs(r.volumes[:2000].sum() - 1.0) < 1e-6 and abs(r.volumes[2000:].sum() - 1.0) < 1e-6
     finally:
         b.close()
+
+
+@pytest.mark.parametrize("radius,group", [(0.05, None), (None, 2), (0.08, 1)])
+def test_radius_and_group_pass_through(T, radius, group):
+    """search_radius and target_group mean what they mean for compute_all."""
+    rng = np.random.default_rng(19)
+    pts = rng.random((4000, 3))
+    groups = (np.arange(len(pts)) % 3).astype(np.uint32)
+    with T.Diagram(pts, groups=groups, container=_box(T)) as d:
+        d.compute_all("fp32", search_radius=radius, target_group=group)
+        vol = d.volumes()
+        offs, nbr, area = d.neighbors_csr()
+        r = d.compute_all_to_host("fp32", search_radius=radius, target_group=group)
+    o2, n2, a2 = r.csr()
+    assert np.array_equal(r.volumes, vol)
+    assert np.array_equal(o2, offs) and np.array_equal(n2, nbr) and np.array_equal(a2, area)
+
+
+@pytest.mark.parametrize("n", [1, 2, 9])
+def test_tiny_diagrams(T, n):
+    import oracle
+
+    pts = np.random.default_rng(20 + n).random((n, 3))
+    ref = oracle.Diagram(pts, lo=[0, 0, 0], hi=[1, 1, 1])
+    rv, ro, ri, _, _, _ = ref.compute_all()
+    with T.Diagram(pts, container=_box(T)) as d:
+        r = d.compute_all_to_host("mixed")
+    offs, nbr, _ = r.csr()
+    assert np.allclose(r.volumes, rv, rtol=1e-11, atol=0)
+    assert np.array_equal(offs.astype(np.int64), ro) and np.array_equal(nbr.astype(np.int64), ri)
+
+
+def test_batch_fp64(T):
+    pts, offs, boxes = _batch_inputs([500, 64, 2000], 80)
+    b = T.Batch(pts, offs, boxes)
+    try:
+        b.compute("fp64")
+        vol = b.volumes()
+        co, cn, ca = b.neighbors_csr()
+        r = b.compute_to_host("fp64")
+        o2, n2, a2 = r.csr()
+        assert np.array_equal(r.volumes, vol)
+        assert np.array_equal(o2, co) and np.array_equal(n2, cn) and np.array_equal(a2, ca)
+    finally:
+        b.close()
